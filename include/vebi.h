@@ -1,0 +1,187 @@
+/*
+ * vebi.h -- C-ABI of the GB300 time-step library for the vebisph ISPH solver.
+ *
+ * The library replaces one call of the Fortran driver:
+ *     call div_free(x_mint,y_mint,x_maxt,y_maxt)        source/base/sph2D_incom.F90:97
+ * whose body is source/base/div_free.F90:22-124.  In the reference every routine of
+ * the step communicates through module globals (source/para/common_2d.F90:20-80); here
+ * the same state lives on the device inside an opaque context, and the host copies the
+ * particle fields in and out through plain pointers.
+ *
+ * Conventions
+ *  - All entry points are extern "C", take plain pointers/sizes and return an int status
+ *    (VEBI_OK == 0).  Warnings are reported in vebi_step_stats.warnings and do not fail.
+ *  - Particle fields use the reference's Fortran layout: a field of shape (npar, m) is m
+ *    contiguous planes of leading dimension `ld` (the reference's npar,
+ *    source/para/common_parameter.F90:5).  tau_p(npar,2,2) is 4 planes ordered
+ *    (1,1),(2,1),(1,2),(2,2).  Particle numbering is the reference's: wall ("boundary")
+ *    particles first (1..nbS), fluid after (nbS+1..npfb); the library never reorders them.
+ *  - Floating point is IEEE binary64 (rkind = c_double, source/para/kind_parameters.F90:11)
+ *    and integers are int32 (ikind = c_int, :12).  The logical(c_bool) `inbin` array is
+ *    one byte per particle.
+ *  - A context owns one CUDA stream and all device memory; it is not thread-safe.
+ *    One host thread drives one context, as the reference's serial main loop does.
+ */
+#ifndef VEBI_H
+#define VEBI_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VEBI_MAX_PATCHES 16
+#define VEBI_MAX_CIRCLES 8
+#define VEBI_NSTAGES 16
+
+/* ---- status codes (each maps to a `stop` site of the reference) ------------------- */
+enum {
+  VEBI_OK = 0,
+  VEBI_ERR_ARG = 1,            /* bad argument / inconsistent sizes                          */
+  VEBI_ERR_CUDA = 2,           /* CUDA runtime or launch error                                */
+  VEBI_ERR_OUT_OF_DOMAIN = 3,  /* neighbour_finding_mod.F90:82-88  (cell index out of range)  */
+  VEBI_ERR_CELL_CAPACITY = 4,  /* neighbour_finding_mod.F90:93-103 (cell population > nplink) */
+  VEBI_ERR_NEIGH_CAPACITY = 5, /* new: the reference overruns ij_link(npfb,nplink) silently   */
+  VEBI_ERR_ALL_IN_BIN = 6,     /* put_in_bin.F90:51-54                                        */
+  VEBI_ERR_MIRROR_CAPACITY = 7,/* new: the reference overruns irelation(npfb+1:npfb+esti)     */
+  VEBI_ERR_TIMEOUT = 8,        /* a bounded device-side wait gave up                          */
+  VEBI_ERR_NO_DEVICE = 9,      /* no usable CUDA device                                       */
+  VEBI_ERR_BOUNDARY = 10       /* check_boundaries failed (input.F90:190-244)                 */
+};
+
+/* warning bits in vebi_step_stats.warnings (the reference prints and continues) */
+enum {
+  VEBI_WARN_BICGSTAB_BREAKDOWN = 1, /* rho == 0, "BICGSTAB Fails" (linear_solver.F90:332-335)  */
+  VEBI_WARN_MAXITER = 2,            /* itermax reached without meeting tol                      */
+  VEBI_WARN_ESCAPEES = 4            /* replace_escapees relocated particles (mirror_..:336-407) */
+};
+
+/* precision modes of the step */
+enum {
+  VEBI_PREC_FP64 = 0,   /* plain FP64 step: the reference's arithmetic                       */
+  VEBI_PREC_MIXED = 1   /* FP32 pair sums/SpMV, FP64 PPE refinement and eigen-step           */
+};
+
+/*
+ * Run parameters.  Field meanings follow INDAT (source/base/input.F90:18-38) and
+ * IBOUND (input.F90:51-81).  Patch and circle arrays are 0-based copies of the
+ * reference's 1-based arrays; patch indices stored in them (b_periodic_parent) keep
+ * the reference's 1-based values.
+ */
+typedef struct vebi_params {
+  /* INDAT */
+  double h, dx, dv;                    /* smoothing length, spacing, particle volume        */
+  double Ra, Pr, El, beta;             /* Rayleigh, Prandtl, elasticity number, visc. ratio */
+  double ve_nonlinearity;              /* PTT epsilon                                       */
+  double alpha_evss;                   /* read but unused by the step                       */
+  double body_force[2];
+  double dt_coef_cfl, dt_coef_visc;
+  double tol;                          /* PPE tolerance; the reference hard-codes 1e-8      */
+  /* padded domain box passed to div_free (sph2D_incom.F90:64-67); all zero = derive it */
+  double x_mint, x_maxt, y_mint, y_maxt;
+  /* IBOUND */
+  double b_node[VEBI_MAX_PATCHES][2];
+  double b_edge[VEBI_MAX_PATCHES][2];
+  double b_vel[VEBI_MAX_PATCHES];
+  double b_thermal[VEBI_MAX_PATCHES];
+  double c_centre[VEBI_MAX_CIRCLES][2];
+  double c_radius[VEBI_MAX_CIRCLES];
+  double c_omega[VEBI_MAX_CIRCLES];
+  double c_vel[VEBI_MAX_CIRCLES][2];
+  double c_thermal[VEBI_MAX_CIRCLES];
+  int32_t b_type[VEBI_MAX_PATCHES];
+  int32_t b_periodic_parent[VEBI_MAX_PATCHES];
+  int32_t nb_patches, nb_circles;
+  /* INDAT integers */
+  int32_t i_open_domain, i_shift_coeff;
+  int32_t npfb, nbS;
+  int32_t const_mod;                   /* 1 Newtonian, 2 linear PTT / Oldroyd-B (Makefile:11-15) */
+  int32_t itermax;                     /* PPE iteration cap; the reference hard-codes 1000       */
+  int32_t nplink;                      /* neighbour / cell capacity; the reference uses 75       */
+  int32_t nmirror_cap;                 /* mirror capacity; 0 = reference estimate 2*npfb         */
+  int32_t precision;                   /* VEBI_PREC_*                                            */
+  int32_t reserved[7];
+} vebi_params;
+
+/* Per-step scalars the Fortran driver and `output` read after div_free
+ * (sph2D_incom.F90:98-117, output.F90:84-85). */
+typedef struct vebi_step_stats {
+  double dt;            /* time step chosen by set_time_step (div_free.F90:126-146)  */
+  double LS_residual;   /* sqrt(|r|^2/|r0|^2) at exit of the PPE solve               */
+  double umax;          /* max |u| used by the CFL bound                             */
+  double max_abs_u, max_abs_v, max_abs_p;   /* TIME file columns (output.F90:84)     */
+  double rms_u;         /* secondary_properties diagnostic (div_free.F90:170-183)    */
+  double ppe_rhs_mean;  /* DC removed from the PPE right-hand side                   */
+  double stage_ms[VEBI_NSTAGES]; /* device time of each stage (0 unless timing on)    */
+  int32_t LS_iters;     /* BiCGSTAB iterations                                       */
+  int32_t n_inbin;
+  int32_t np, npfb, nmirror, maxneighbours;
+  int32_t n_escapees;
+  int32_t error;        /* first device-side error code of the step (0 = none)       */
+  int32_t warnings;     /* VEBI_WARN_* bits                                          */
+  int32_t gpu_launches; /* kernels this library launched during the step             */
+  int32_t refine_iters; /* mixed precision: outer refinement sweeps                  */
+  int32_t pad;
+} vebi_step_stats;
+
+typedef struct vebi_ctx vebi_ctx;
+
+/* Allocate device state for up to npfb particles plus mirrors and build the cell grid
+ * (cell_generator, cell_griddin.F90:13-24; kernel constants, input.F90:164-172;
+ * corner angles, check_boundaries input.F90:182-273).  Replaces getdata's setup. */
+int vebi_create(const vebi_params* params, vebi_ctx** out);
+
+/* Copy the host particle state into the context: the arrays getdata fills
+ * (input.F90:105-145).  tau_p and trace_conf may be NULL for const_mod == 1;
+ * inbin may be NULL (all false).  ld >= npfb. */
+int vebi_upload_state(vebi_ctx* ctx, const double* r, const double* u, const double* tau_p,
+                      const double* theta, const double* trace_conf, const uint8_t* inbin,
+                      int32_t ld);
+
+/* One time step: the div_free equivalent (div_free.F90:22-124).  `secondary` = 1 runs
+ * secondary_properties' vorticity/rms diagnostic (done at dump times, div_free.F90:154).
+ * stats may be NULL. */
+int vebi_step(vebi_ctx* ctx, double x_mint, double y_mint, double x_maxt, double y_maxt,
+              int32_t secondary, vebi_step_stats* stats);
+
+/* Run nsteps steps back to back on the context's stream (no host copies) and return
+ * the device time between the first launch and the last completion in *ms. */
+int vebi_run_steps(vebi_ctx* ctx, double x_mint, double y_mint, double x_maxt, double y_maxt,
+                   int32_t nsteps, double* ms, vebi_step_stats* last);
+
+/* Copy particle fields back to the host, for dumps (output.F90:44-51,66-72).
+ * Any pointer may be NULL to skip that field.  Fields of fluid/wall particles only
+ * (1..npfb), in the host's layout with leading dimension ld. */
+int vebi_download_state(vebi_ctx* ctx, double* r, double* u, double* tau_p, double* theta,
+                        double* p, double* vort, double* a_out, double* trace_conf,
+                        int32_t* n_surf, uint8_t* inbin, int32_t ld);
+
+/* Free device state. */
+int vebi_destroy(vebi_ctx* ctx);
+
+/* Page-lock (pin) a host array the caller owns, e.g. the Fortran r/u/tau_p arrays, so the
+ * transfers of vebi_upload_state / vebi_download_state run at full link speed; and undo it. */
+int vebi_pin_host(void* ptr, int64_t bytes);
+int vebi_unpin_host(void* ptr);
+
+/* Turn per-stage CUDA-event timing on (1) or off (0). */
+int vebi_set_timing(vebi_ctx* ctx, int32_t on);
+
+/* Intermediate arrays of the last step, for parity tests against the CPU oracle:
+ * name -> element size and count (vebi_debug_size) and a host copy (vebi_debug_get).
+ * Names: see vebisph_gb300/solver.py (DEBUG_FIELDS). */
+int vebi_debug_size(vebi_ctx* ctx, const char* name, int64_t* elem_bytes, int64_t* count);
+int vebi_debug_get(vebi_ctx* ctx, const char* name, void* out, int64_t bytes);
+
+/* Static description of the library build. */
+const char* vebi_version(void);
+
+/* Last error message of this thread (static storage). */
+const char* vebi_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VEBI_H */

@@ -1,0 +1,123 @@
+"""ctypes wrapper of the CPU oracle (test infrastructure only).
+
+Mirrors the GPU solver's host API (vebisph_gb300.solver.StepSolver) so parity tests can
+drive both the same way: create from a Case, upload, step, read fields and intermediates.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from vebisph_gb300 import abi
+from . import build as _build
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        lib = C.CDLL(str(_build.build()))
+        vp = C.c_void_p
+        P = C.POINTER
+        lib.orc_create.argtypes = [P(abi.VebiParams), P(C.c_int)]
+        lib.orc_create.restype = vp
+        lib.orc_destroy.argtypes = [vp]
+        lib.orc_set_state.argtypes = [vp, P(C.c_double), P(C.c_double), P(C.c_double), P(C.c_double),
+                                      P(C.c_double), P(C.c_uint8), C.c_int]
+        lib.orc_step.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
+                                 P(abi.VebiStepStats)]
+        lib.orc_box.argtypes = [vp, P(C.c_double), P(C.c_int)]
+        lib.orc_size.argtypes = [vp, C.c_char_p, P(C.c_int64), P(C.c_int64)]
+        lib.orc_get.argtypes = [vp, C.c_char_p, vp, C.c_int64]
+        lib.orc_kernel_w.argtypes = [vp, C.c_double]
+        lib.orc_kernel_w.restype = C.c_double
+        lib.orc_kernel_fac.argtypes = [vp, C.c_double]
+        lib.orc_kernel_fac.restype = C.c_double
+        lib.orc_eigens.argtypes = [P(C.c_double), P(C.c_double), P(C.c_double)]
+        lib.orc_threads.restype = C.c_int
+        _lib = lib
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+class OracleSolver:
+    """One oracle context holding a Case's state."""
+
+    def __init__(self, case, precision: int = abi.PREC_FP64):
+        self.lib = load()
+        self.case = case
+        self.params = case.params(precision)
+        st = C.c_int(0)
+        self.h = self.lib.orc_create(C.byref(self.params), C.byref(st))
+        if not self.h:
+            raise RuntimeError(f"oracle create failed: {abi.STATUS_NAMES.get(st.value, st.value)}")
+        box = (C.c_double * 4)()
+        nc = (C.c_int * 2)()
+        self.lib.orc_box(self.h, box, nc)
+        self.x_mint, self.x_maxt, self.y_mint, self.y_maxt = list(box)
+        self.ncx, self.ncy = list(nc)
+        f = case.fortran_planes()
+        self.upload(f["r"], f["u"], f["tau"], f["theta"], f["trace_conf"], f["inbin"], f["ld"])
+
+    def upload(self, r, u, tau, theta, trace_conf, inbin, ld):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (r, u, tau, theta, trace_conf)]
+        ib = np.ascontiguousarray(inbin, dtype=np.uint8)
+        st = self.lib.orc_set_state(self.h, *[_dp(a) for a in arrs],
+                                    ib.ctypes.data_as(C.POINTER(C.c_uint8)), ld)
+        if st:
+            raise RuntimeError(f"oracle set_state: {abi.STATUS_NAMES.get(st, st)}")
+
+    def step(self, secondary: bool = False) -> dict:
+        s = abi.VebiStepStats()
+        st = self.lib.orc_step(self.h, self.x_mint, self.y_mint, self.x_maxt, self.y_maxt,
+                               int(secondary), C.byref(s))
+        d = s.as_dict()
+        d["status"] = st
+        if st:
+            raise RuntimeError(f"oracle step: {abi.STATUS_NAMES.get(st, st)}")
+        return d
+
+    def get(self, name: str) -> np.ndarray:
+        esz, n = C.c_int64(), C.c_int64()
+        if self.lib.orc_size(self.h, name.encode(), C.byref(esz), C.byref(n)):
+            raise KeyError(name)
+        dt = np.float64 if esz.value == 8 else np.int32
+        out = np.empty(n.value, dt)
+        self.lib.orc_get(self.h, name.encode(), out.ctypes.data_as(C.c_void_p), out.nbytes)
+        return out
+
+    def W(self, q: float) -> float:
+        return self.lib.orc_kernel_w(self.h, q)
+
+    def fac(self, q: float) -> float:
+        return self.lib.orc_kernel_fac(self.h, q)
+
+    def close(self):
+        if self.h:
+            self.lib.orc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def eigens(A):
+    """calc_eigens on a 2x2 matrix given as [[a11,a12],[a21,a22]]."""
+    lib = load()
+    a = np.ascontiguousarray(np.asarray(A, float).ravel())
+    L = np.zeros(2)
+    R = np.zeros(4)
+    lib.orc_eigens(_dp(a), _dp(L), _dp(R))
+    return L, R.reshape(2, 2)
+
+
+def threads() -> int:
+    return load().orc_threads()

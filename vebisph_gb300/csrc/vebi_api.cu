@@ -1,0 +1,547 @@
+// vebi_api.cu -- the C-ABI of include/vebi.h: context set-up, state transfer, the step
+// orchestration (div_free, div_free.F90:22-124) and the inspection entry points.
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "vebi_ctx.cuh"
+
+namespace vebi {
+
+int ppe_solver_blocks(int device, int nsm);
+
+static thread_local std::string g_err;
+
+static double bits_to_double_host(unsigned long long b) {
+  double v;
+  std::memcpy(&v, &b, sizeof(v));
+  return v;
+}
+
+static int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                              \
+  do {                                                                              \
+    cudaError_t e_ = (expr);                                                        \
+    if (e_ != cudaSuccess)                                                          \
+      return fail(VEBI_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// host copy of the quintic spline (sphtools.F90:46-76) for the shifting constant Wab(dx/h)
+static double host_wab(double ad_7, double qq) {
+  auto p5 = [](double x) { double x2 = x * x; double x3 = x * x2; return x2 * x3; };
+  int isel = (int)std::floor(qq);
+  if (isel == 0) return ad_7 * (p5(3.0 - qq) - 6.0 * p5(2.0 - qq) + 15.0 * p5(1.0 - qq));
+  if (isel == 1) return ad_7 * (p5(3.0 - qq) - 6.0 * p5(2.0 - qq));
+  if (isel == 2) return ad_7 * p5(3.0 - qq);
+  return 0.0;
+}
+
+template <class T>
+static int dalloc(Ctx& x, T** p, size_t n) {
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  if (e != cudaSuccess) return fail(VEBI_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  x.allocs.push_back((void*)*p);
+  cudaMemset(*p, 0, n * sizeof(T));
+  return VEBI_OK;
+}
+
+// check_boundaries (input.F90:182-273) and the run constants (input.F90:164-172)
+static int build_consts(Ctx& x) {
+  const vebi_params& P = x.prm;
+  Consts& c = x.c;
+  std::memset(&c, 0, sizeof(c));
+  if (P.npfb <= 0 || P.nbS < 0 || P.nbS > P.npfb) return fail(VEBI_ERR_ARG, "npfb/nbS out of range");
+  if (P.nb_patches < 0 || P.nb_patches > VEBI_MAX_PATCHES) return fail(VEBI_ERR_ARG, "nb_patches out of range");
+  if (P.nb_circles < 0 || P.nb_circles > VEBI_MAX_CIRCLES) return fail(VEBI_ERR_ARG, "nb_circles out of range");
+  if (!(P.h > 0.0) || !(P.dv > 0.0)) return fail(VEBI_ERR_ARG, "h and dv must be positive");
+  const int nb = P.nb_patches;
+  c.nb = nb;
+  c.ncirc = P.nb_circles;
+  c.h = P.h;
+  c.dx = P.dx;
+  c.dv = P.dv;
+  c.sup_size = 3.0 * c.h;
+  c.sup_size_2 = 9.0 * (c.h * c.h);
+  c.uno_sup_size = 1.0 / (3.0 * c.h);
+  c.ad_7 = 7.0 / 478.0 / PI / c.h / c.h;
+  c.ad_7h = c.ad_7 / c.h;
+  c.eta2 = c.h * c.h * 1.0e-10;
+  c.eta_small = (double)0.01f * c.h * c.h;  // default-real literal (kernel_calculation.F90:36)
+  c.oneoverh = 1.0 / c.h;
+  c.Ra = P.Ra;
+  c.Pr = P.Pr;
+  c.El = P.El;
+  c.beta = P.beta;
+  c.eps_ptt = P.ve_nonlinearity;
+  c.Wi = P.El * std::sqrt(P.Ra / P.Pr);
+  c.bf[0] = P.body_force[0];
+  c.bf[1] = P.body_force[1];
+  c.dt_coef_cfl = P.dt_coef_cfl;
+  c.dt_coef_visc = P.dt_coef_visc;
+  c.dt_visc = P.dt_coef_visc * c.h * c.h * std::fmin(std::sqrt(P.Ra / P.Pr), std::sqrt(P.Ra * P.Pr));
+  c.coeff_solvent = P.beta * std::sqrt(P.Pr / P.Ra);
+  c.coeff_polymeric = (1.0 - P.beta) * P.Pr / (P.Ra * P.El);
+  c.coeff_theta = 1.0 / std::sqrt(P.Ra * P.Pr);
+  c.wab1 = host_wab(c.ad_7, c.dx / c.h);
+  c.tol = P.tol > 0 ? P.tol : 1.0e-8;
+  c.itermax = P.itermax > 0 ? P.itermax : 1000;
+  c.nplink = P.nplink > 0 ? P.nplink : 75;
+  if (c.nplink > 96) return fail(VEBI_ERR_ARG, "nplink above 96 is not supported");
+  c.open_domain = P.i_open_domain;
+  c.shift_coeff = P.i_shift_coeff;
+  c.const_mod = P.const_mod == 1 ? 1 : 2;
+  c.npfb = P.npfb;
+  c.nbS = P.nbS;
+  for (int i = 0; i < nb; ++i) {
+    for (int q = 0; q < 2; ++q) { c.b_node[i][q] = P.b_node[i][q]; c.b_edge[i][q] = P.b_edge[i][q]; }
+    c.b_vel[i] = P.b_vel[i];
+    c.b_thermal[i] = P.b_thermal[i];
+    c.b_type[i] = P.b_type[i];
+    c.b_pp[i] = P.b_periodic_parent[i] - 1;
+    c.b_elen[i] = std::sqrt(P.b_edge[i][0] * P.b_edge[i][0] + P.b_edge[i][1] * P.b_edge[i][1]);
+  }
+  for (int i = 0; i < c.ncirc; ++i) {
+    c.c_centre[i][0] = P.c_centre[i][0];
+    c.c_centre[i][1] = P.c_centre[i][1];
+    c.c_radius[i] = P.c_radius[i];
+    c.c_omega[i] = P.c_omega[i];
+    c.c_vel[i][0] = P.c_vel[i][0];
+    c.c_vel[i][1] = P.c_vel[i][1];
+    c.c_thermal[i] = P.c_thermal[i];
+  }
+  // checks 1-3 of check_boundaries
+  int n_fail = 0;
+  for (int i = 0; i < nb; ++i) {
+    int j = (i == nb - 1) ? 0 : i + 1;
+    double t1 = P.b_node[i][0] + P.b_edge[i][0] - P.b_node[j][0];
+    double t2 = P.b_node[i][1] + P.b_edge[i][1] - P.b_node[j][1];
+    if (std::sqrt(t1 * t1 + t2 * t2) > 1.0e-10) ++n_fail;
+  }
+  double s1 = 0.0, s2 = 0.0;
+  for (int i = 0; i < nb; ++i) { s1 += P.b_edge[i][0]; s2 += P.b_edge[i][1]; }
+  if (nb > 0 && std::sqrt(s1 * s1 + s2 * s2) > 1.0e-10) ++n_fail;
+  for (int i = 0; i < nb; ++i) {
+    if (P.b_type[i] == 2) {
+      int pp = P.b_periodic_parent[i] - 1;
+      if (pp < 0 || pp >= nb) { ++n_fail; continue; }
+      double t1 = P.b_edge[i][0] + P.b_edge[pp][0], t2 = P.b_edge[i][1] + P.b_edge[pp][1];
+      if (std::fabs(std::sqrt(t1 * t1 + t2 * t2)) > 1.0e-10) ++n_fail;
+    }
+  }
+  if (n_fail) return fail(VEBI_ERR_BOUNDARY, "check_boundaries failed");
+  // check 4: corner angles; rotation matrices of periodic pairs (angle_between_patches)
+  for (int i = 0; i < nb; ++i) {
+    int ibm1 = (i + nb - 1) % nb, ibp1 = (i + 1) % nb;
+    double p_dist = P.b_edge[ibm1][1] * P.b_node[ibp1][0] - P.b_edge[ibm1][0] * P.b_node[ibp1][1] +
+                    P.b_node[i][0] * P.b_node[ibm1][1] - P.b_node[i][1] * P.b_node[ibm1][0];
+    p_dist = -1.0 * p_dist / std::sqrt(P.b_edge[ibm1][0] * P.b_edge[ibm1][0] + P.b_edge[ibm1][1] * P.b_edge[ibm1][1]);
+    double tmp1 = std::sqrt(P.b_edge[i][0] * P.b_edge[i][0] + P.b_edge[i][1] * P.b_edge[i][1]);
+    if (p_dist <= 0.0 && std::fabs(p_dist) > std::fabs(tmp1)) p_dist = -tmp1;
+    else if (p_dist > 0.0 && std::fabs(p_dist) > std::fabs(tmp1)) p_dist = tmp1;
+    c.b_corner_angle[i] = std::asin(p_dist / tmp1);
+    if (P.b_type[i] == 2) {
+      int b = P.b_periodic_parent[i] - 1;
+      double ta = P.b_edge[i][0] * P.b_edge[b][0] + P.b_edge[i][1] * P.b_edge[b][1];
+      double na = P.b_edge[i][0] * P.b_edge[i][0] + P.b_edge[i][1] * P.b_edge[i][1];
+      double nbb = P.b_edge[b][0] * P.b_edge[b][0] + P.b_edge[b][1] * P.b_edge[b][1];
+      double t = ta / std::sqrt(na * nbb);
+      t = std::acos(t) - PI;
+      c.b_rot[i][0] = std::cos(t);
+      c.b_rot[i][1] = -std::sin(t);
+      c.b_rot[i][2] = std::sin(t);
+      c.b_rot[i][3] = std::cos(t);
+    }
+  }
+  // padded box (sph2D_incom.F90:64-67) and cell grid (cell_griddin.F90:13-24)
+  double xmn = P.x_mint, xmx = P.x_maxt, ymn = P.y_mint, ymx = P.y_maxt;
+  if (xmn == 0.0 && xmx == 0.0 && ymn == 0.0 && ymx == 0.0) {
+    double xb_min = 1e300, xb_max = -1e300, yb_min = 1e300, yb_max = -1e300;
+    for (int i = 0; i < nb; ++i) {
+      xb_min = std::fmin(xb_min, P.b_node[i][0]); xb_max = std::fmax(xb_max, P.b_node[i][0]);
+      yb_min = std::fmin(yb_min, P.b_node[i][1]); yb_max = std::fmax(yb_max, P.b_node[i][1]);
+    }
+    xmn = xb_min - c.sup_size * 1.5; xmx = xb_max + c.sup_size * 1.5;
+    ymn = yb_min - c.sup_size * 1.5; ymx = yb_max + c.sup_size * 1.5;
+  }
+  c.x_mint = xmn; c.x_maxt = xmx; c.y_mint = ymn; c.y_maxt = ymx;
+  double fx = (xmx - xmn) * c.uno_sup_size, fy = (ymx - ymn) * c.uno_sup_size;
+  if (!(fx >= 0.0 && fy >= 0.0 && fx < 1.0e8 && fy < 1.0e8)) return fail(VEBI_ERR_ARG, "bad domain box");
+  c.ncx = (int)fx + 1;
+  c.ncy = (int)fy + 1;
+  long long nct = (long long)c.ncx * c.ncy;
+  if (nct > 400000000LL) return fail(VEBI_ERR_ARG, "cell grid too large");
+  c.nct = (int)nct;
+  // mirror capacity: create_mirror_particles' estimate (mirror_boundaries_mod.F90:53-54)
+  c.mcap = P.nmirror_cap > 0 ? P.nmirror_cap : (P.npfb <= 500 ? 10 * P.npfb : 2 * P.npfb);
+  c.cap = c.npfb + c.mcap;
+  return VEBI_OK;
+}
+
+static int allocate_all(Ctx& x) {
+  Consts& c = x.c;
+  Dev& d = x.d;
+  const size_t cap = (size_t)c.cap, n = (size_t)c.npfb, E = (size_t)c.nplink * n;
+  int st = 0;
+#define A_(p, cnt) if ((st = dalloc(x, &(p), (cnt)))) return st
+  A_(d.s, 1);
+  A_(d.rx, cap); A_(d.ry, cap); A_(d.ux, cap); A_(d.uy, cap); A_(d.th, cap);
+  A_(d.rx2, cap); A_(d.ry2, cap); A_(d.ux2, cap); A_(d.uy2, cap); A_(d.th2, cap);
+  A_(d.r0x, n); A_(d.r0y, n); A_(d.u0x, n); A_(d.u0y, n);
+  A_(d.p, cap);
+  for (int q = 0; q < 4; ++q) A_(d.tau[q], cap);
+  A_(d.trace_conf, n); A_(d.a_out, n); A_(d.vort, n);
+  A_(d.n_surf, cap); A_(d.inbin, cap);
+  A_(d.irel, cap); A_(d.vrel, cap); A_(d.dP_mp, cap);
+  A_(d.cellpart, cap); A_(d.cell_fill, cap); A_(d.ip, cap);
+  A_(d.cell_cnt, (size_t)c.nct); A_(d.cell_start, (size_t)c.nct + 1);
+  A_(d.scan_part, (size_t)c.nct / 1024 + 2);
+  size_t sel_items = (size_t)(c.npfb > c.mcap ? c.npfb : c.mcap);
+  A_(d.sel_blk, sel_items / SEL_CH + 2);
+  A_(d.ij_count, n); A_(d.ij_link, E);
+  A_(d.wGx, E); A_(d.wGy, E); A_(d.wL, E);
+  for (int q = 0; q < 4; ++q) A_(d.kgcm[q], n);
+  for (int q = 0; q < 6; ++q) A_(d.grad[q], cap);
+  A_(d.gradCx, n); A_(d.gradCy, n); A_(d.ushx, n); A_(d.ushy, n);
+  if (c.open_domain == 1) {
+    A_(d.conc, n); A_(d.div_r, n); A_(d.surf_nx, n); A_(d.surf_ny, n); A_(d.ppe_smooth, n);
+    A_(d.beta_div_r, n);
+  }
+  A_(d.ppe_B, n); A_(d.ppe_diag, n); A_(d.ppe_val, E); A_(d.ppe_col, E);
+  A_(d.bx, n); A_(d.br, n); A_(d.brb, n); A_(d.bv, n); A_(d.bp, n); A_(d.bpi, n);
+  A_(d.bs, n); A_(d.bsi, n); A_(d.bt, n);
+  size_t np_part = (size_t)grid_for(c.npfb);
+  size_t coop_part = (size_t)x.coop_blocks * 12;
+  A_(d.partials, (np_part > coop_part ? np_part : coop_part) + 64);
+  A_(d.gpx, n); A_(d.gpy, n);
+#undef A_
+  return VEBI_OK;
+}
+
+}  // namespace vebi
+
+using namespace vebi;
+
+struct vebi_ctx {
+  Ctx x;
+};
+
+extern "C" {
+
+const char* vebi_version(void) {
+  return "vebisph-gb300 step library: FP64 div_free on sm_103a (ELL pair lists, persistent BiCGSTAB)";
+}
+
+const char* vebi_last_error(void) { return g_err.c_str(); }
+
+int vebi_create(const vebi_params* params, vebi_ctx** out) {
+  if (!params || !out) return fail(VEBI_ERR_ARG, "null argument");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(VEBI_ERR_NO_DEVICE, "no CUDA device");
+  auto* h = new vebi_ctx();
+  Ctx& x = h->x;
+  x.prm = *params;
+  x.precision = params->precision;
+  int st = build_consts(x);
+  if (st) { delete h; return st; }
+  cudaGetDevice(&x.device);
+  cudaDeviceGetAttribute(&x.nsm, cudaDevAttrMultiProcessorCount, x.device);
+  x.coop_blocks = ppe_solver_blocks(x.device, x.nsm);
+  x.gs_blocks = x.nsm * 8;
+  if (cudaStreamCreateWithFlags(&x.st, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return fail(VEBI_ERR_CUDA, "cudaStreamCreate failed");
+  }
+  for (int i = 0; i <= VEBI_NSTAGES; ++i) cudaEventCreate(&x.ev[i]);
+  st = allocate_all(x);
+  if (st) { vebi_destroy(h); return st; }
+  // trace of the conformation tensor starts at 2 (input.F90:111)
+  std::vector<double> two((size_t)x.c.npfb, 2.0);
+  cudaMemcpy(x.d.trace_conf, two.data(), two.size() * sizeof(double), cudaMemcpyHostToDevice);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) { vebi_destroy(h); return fail(VEBI_ERR_CUDA, cudaGetErrorString(e)); }
+  *out = h;
+  return VEBI_OK;
+}
+
+int vebi_upload_state(vebi_ctx* h, const double* r, const double* u, const double* tau_p, const double* theta,
+                      const double* trace_conf, const uint8_t* inbin, int32_t ld) {
+  if (!h || !r || !u) return fail(VEBI_ERR_ARG, "null argument");
+  Ctx& x = h->x;
+  const int n = x.c.npfb;
+  if (ld < n) return fail(VEBI_ERR_ARG, "ld < npfb");
+  const size_t B = sizeof(double) * (size_t)n;
+  Dev& d = x.d;
+  CUDA_TRY(cudaMemcpyAsync(d.rx, r, B, cudaMemcpyHostToDevice, x.st));
+  CUDA_TRY(cudaMemcpyAsync(d.ry, r + ld, B, cudaMemcpyHostToDevice, x.st));
+  CUDA_TRY(cudaMemcpyAsync(d.ux, u, B, cudaMemcpyHostToDevice, x.st));
+  CUDA_TRY(cudaMemcpyAsync(d.uy, u + ld, B, cudaMemcpyHostToDevice, x.st));
+  if (theta) CUDA_TRY(cudaMemcpyAsync(d.th, theta, B, cudaMemcpyHostToDevice, x.st));
+  else CUDA_TRY(cudaMemsetAsync(d.th, 0, B, x.st));
+  for (int q = 0; q < 4; ++q) {
+    if (tau_p) CUDA_TRY(cudaMemcpyAsync(d.tau[q], tau_p + (size_t)q * ld, B, cudaMemcpyHostToDevice, x.st));
+    else CUDA_TRY(cudaMemsetAsync(d.tau[q], 0, B, x.st));
+  }
+  if (trace_conf) CUDA_TRY(cudaMemcpyAsync(d.trace_conf, trace_conf, B, cudaMemcpyHostToDevice, x.st));
+  if (inbin) CUDA_TRY(cudaMemcpyAsync(d.inbin, inbin, (size_t)n, cudaMemcpyHostToDevice, x.st));
+  else CUDA_TRY(cudaMemsetAsync(d.inbin, 0, (size_t)n, x.st));
+  x.have_state = true;
+  return VEBI_OK;
+}
+
+static int finish_step(Ctx& x, vebi_step_stats* stats, bool sync) {
+  Scal s;
+  CUDA_TRY(cudaMemcpyAsync(&s, x.d.s, sizeof(Scal), cudaMemcpyDeviceToHost, x.st));
+  if (x.timing) cudaEventRecord(x.ev[VEBI_NSTAGES], x.st);
+  if (sync) CUDA_TRY(cudaStreamSynchronize(x.st));
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(VEBI_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  vebi_step_stats o;
+  std::memset(&o, 0, sizeof(o));
+  o.dt = s.dt;
+  o.LS_residual = s.ls_residual;
+  o.umax = bits_to_double_host(s.umax_bits);
+  o.max_abs_u = bits_to_double_host(s.absu_bits);
+  o.max_abs_v = bits_to_double_host(s.absv_bits);
+  o.max_abs_p = bits_to_double_host(s.absp_bits);
+  o.rms_u = s.rms_u;
+  o.ppe_rhs_mean = s.rhs_mean;
+  o.LS_iters = s.ls_iters;
+  o.n_inbin = s.n_inbin;
+  o.np = s.np;
+  o.npfb = x.c.npfb;
+  o.nmirror = s.nmirror;
+  o.maxneighbours = s.maxneigh;
+  o.n_escapees = s.n_escapees;
+  o.error = s.error;
+  o.warnings = s.warnings | (s.n_escapees ? VEBI_WARN_ESCAPEES : 0);
+  o.gpu_launches = x.launches;
+  o.refine_iters = s.refine_iters;
+  if (x.timing && sync) {
+    int prev = -1;
+    for (int q = 0; q <= VEBI_NSTAGES; ++q) {
+      bool used = q == VEBI_NSTAGES || x.ev_used[q];
+      if (!used) continue;
+      if (prev >= 0) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, x.ev[prev], x.ev[q]);
+        o.stage_ms[prev] = ms;
+      }
+      prev = q;
+    }
+  }
+  x.last = o;
+  if (stats) *stats = o;
+  if (s.error) return fail(s.error, "device-side error in the step");
+  if (s.n_inbin == x.c.npfb - x.c.nbS && x.c.npfb > x.c.nbS) return fail(VEBI_ERR_ALL_IN_BIN, "all liquid particles are in the bin");
+  return VEBI_OK;
+}
+
+static void enqueue_step(Ctx& x, int secondary) {
+  for (int q = 0; q < VEBI_NSTAGES; ++q) x.ev_used[q] = false;
+  stage_mark(x, 0);
+  launch_advect_bin(x);
+  stage_mark(x, 1);
+  launch_mirrors(x);
+  stage_mark(x, 2);
+  launch_cells_neighbours(x);
+  stage_mark(x, 4);
+  launch_weights_surface_shift(x);
+  launch_predictor(x);
+  launch_ppe(x);
+  launch_final(x, secondary);
+}
+
+int vebi_step(vebi_ctx* h, double x_mint, double y_mint, double x_maxt, double y_maxt, int32_t secondary,
+              vebi_step_stats* stats) {
+  if (!h) return fail(VEBI_ERR_ARG, "null context");
+  Ctx& x = h->x;
+  if (!x.have_state) return fail(VEBI_ERR_ARG, "no state uploaded");
+  if (x_mint != x.c.x_mint || x_maxt != x.c.x_maxt || y_mint != x.c.y_mint || y_maxt != x.c.y_maxt)
+    return fail(VEBI_ERR_ARG, "domain box differs from the one the context was created with");
+  x.launches = 0;
+  enqueue_step(x, secondary);
+  return finish_step(x, stats, true);
+}
+
+int vebi_run_steps(vebi_ctx* h, double x_mint, double y_mint, double x_maxt, double y_maxt, int32_t nsteps,
+                   double* ms, vebi_step_stats* last) {
+  if (!h || nsteps < 0) return fail(VEBI_ERR_ARG, "bad argument");
+  Ctx& x = h->x;
+  if (!x.have_state) return fail(VEBI_ERR_ARG, "no state uploaded");
+  if (x_mint != x.c.x_mint || x_maxt != x.c.x_maxt || y_mint != x.c.y_mint || y_maxt != x.c.y_maxt)
+    return fail(VEBI_ERR_ARG, "domain box differs from the one the context was created with");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  bool timing = x.timing;
+  x.timing = false;
+  x.launches = 0;
+  cudaEventRecord(e0, x.st);
+  for (int s = 0; s < nsteps; ++s) enqueue_step(x, 0);
+  cudaEventRecord(e1, x.st);
+  int st = finish_step(x, last, true);
+  float t = 0.f;
+  cudaEventElapsedTime(&t, e0, e1);
+  if (ms) *ms = t;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  x.timing = timing;
+  return st;
+}
+
+int vebi_download_state(vebi_ctx* h, double* r, double* u, double* tau_p, double* theta, double* p, double* vort,
+                        double* a_out, double* trace_conf, int32_t* n_surf, uint8_t* inbin, int32_t ld) {
+  if (!h) return fail(VEBI_ERR_ARG, "null context");
+  Ctx& x = h->x;
+  const int n = x.c.npfb;
+  if (ld < n) return fail(VEBI_ERR_ARG, "ld < npfb");
+  const size_t B = sizeof(double) * (size_t)n;
+  Dev& d = x.d;
+  if (r) {
+    CUDA_TRY(cudaMemcpyAsync(r, d.rx, B, cudaMemcpyDeviceToHost, x.st));
+    CUDA_TRY(cudaMemcpyAsync(r + ld, d.ry, B, cudaMemcpyDeviceToHost, x.st));
+  }
+  if (u) {
+    CUDA_TRY(cudaMemcpyAsync(u, d.ux, B, cudaMemcpyDeviceToHost, x.st));
+    CUDA_TRY(cudaMemcpyAsync(u + ld, d.uy, B, cudaMemcpyDeviceToHost, x.st));
+  }
+  if (tau_p)
+    for (int q = 0; q < 4; ++q) CUDA_TRY(cudaMemcpyAsync(tau_p + (size_t)q * ld, d.tau[q], B, cudaMemcpyDeviceToHost, x.st));
+  if (theta) CUDA_TRY(cudaMemcpyAsync(theta, d.th, B, cudaMemcpyDeviceToHost, x.st));
+  if (p) CUDA_TRY(cudaMemcpyAsync(p, d.p, B, cudaMemcpyDeviceToHost, x.st));
+  if (vort) CUDA_TRY(cudaMemcpyAsync(vort, d.vort, B, cudaMemcpyDeviceToHost, x.st));
+  if (a_out) CUDA_TRY(cudaMemcpyAsync(a_out, d.a_out, B, cudaMemcpyDeviceToHost, x.st));
+  if (trace_conf) CUDA_TRY(cudaMemcpyAsync(trace_conf, d.trace_conf, B, cudaMemcpyDeviceToHost, x.st));
+  if (n_surf) CUDA_TRY(cudaMemcpyAsync(n_surf, d.n_surf, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, x.st));
+  if (inbin) CUDA_TRY(cudaMemcpyAsync(inbin, d.inbin, (size_t)n, cudaMemcpyDeviceToHost, x.st));
+  CUDA_TRY(cudaStreamSynchronize(x.st));
+  return VEBI_OK;
+}
+
+int vebi_destroy(vebi_ctx* h) {
+  if (!h) return VEBI_OK;
+  Ctx& x = h->x;
+  if (x.st) cudaStreamSynchronize(x.st);
+  for (void* p : x.allocs) cudaFree(p);
+  x.allocs.clear();
+  for (int i = 0; i <= VEBI_NSTAGES; ++i)
+    if (x.ev[i]) cudaEventDestroy(x.ev[i]);
+  if (x.st) cudaStreamDestroy(x.st);
+  delete h;
+  return VEBI_OK;
+}
+
+int vebi_pin_host(void* ptr, int64_t bytes) {
+  if (!ptr || bytes <= 0) return fail(VEBI_ERR_ARG, "bad argument");
+  CUDA_TRY(cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault));
+  return VEBI_OK;
+}
+
+int vebi_unpin_host(void* ptr) {
+  if (!ptr) return fail(VEBI_ERR_ARG, "null pointer");
+  CUDA_TRY(cudaHostUnregister(ptr));
+  return VEBI_OK;
+}
+
+int vebi_set_timing(vebi_ctx* h, int32_t on) {
+  if (!h) return fail(VEBI_ERR_ARG, "null context");
+  h->x.timing = on != 0;
+  return VEBI_OK;
+}
+
+// ------------------------------------------------------------------ inspection
+struct DView { const void* p; int64_t esz, n; };
+
+static DView dview(Ctx& x, const std::string& nm) {
+  Dev& d = x.d;
+  const Consts& c = x.c;
+  Scal s;
+  cudaMemcpy(&s, d.s, sizeof(Scal), cudaMemcpyDeviceToHost);
+  const int64_t np = s.np, n = c.npfb, nm_ = s.nmirror;
+  const int64_t ell = (int64_t)(s.maxneigh > 0 ? s.maxneigh : 1) * n;
+  auto D = [](const double* p, int64_t k) { return DView{p, 8, k}; };
+  auto I = [](const int* p, int64_t k) { return DView{p, 4, k}; };
+  if (nm == "rx") return D(d.rx, n);
+  if (nm == "ry") return D(d.ry, n);
+  if (nm == "ux") return D(d.ux, n);
+  if (nm == "uy") return D(d.uy, n);
+  if (nm == "theta") return D(d.th, n);
+  if (nm == "p") return D(d.p, np);
+  if (nm == "tau11") return D(d.tau[0], np);
+  if (nm == "tau21") return D(d.tau[1], np);
+  if (nm == "tau12") return D(d.tau[2], np);
+  if (nm == "tau22") return D(d.tau[3], np);
+  if (nm == "trace_conf") return D(d.trace_conf, n);
+  if (nm == "a_out") return D(d.a_out, n);
+  if (nm == "vort") return D(d.vort, n);
+  if (nm == "n_surf") return I(d.n_surf, np);
+  if (nm == "irelation") return I(d.irel + n, nm_);
+  if (nm == "vrelation") return I(d.vrel + n, nm_);
+  if (nm == "dP_mp") return D(d.dP_mp + n, nm_);
+  if (nm == "rsx") return D(d.rx2, np);
+  if (nm == "rsy") return D(d.ry2, np);
+  if (nm == "cellpart") return I(d.cellpart, np);
+  if (nm == "ist") return I(d.cell_start, (int64_t)c.nct + 1);
+  if (nm == "cell_cnt") return I(d.cell_cnt, (int64_t)c.nct);
+  if (nm == "ij_count") return I(d.ij_count, n);
+  if (nm == "ij_link") return I(d.ij_link, ell);
+  if (nm == "w_Gx") return D(d.wGx, ell);
+  if (nm == "w_Gy") return D(d.wGy, ell);
+  if (nm == "w_L") return D(d.wL, ell);
+  if (nm == "kgcm11") return D(d.kgcm[0], n);
+  if (nm == "kgcm21") return D(d.kgcm[1], n);
+  if (nm == "kgcm12") return D(d.kgcm[2], n);
+  if (nm == "kgcm22") return D(d.kgcm[3], n);
+  if (nm == "gradu_x") return D(d.grad[0], np);
+  if (nm == "gradu_y") return D(d.grad[1], np);
+  if (nm == "gradv_x") return D(d.grad[2], np);
+  if (nm == "gradv_y") return D(d.grad[3], np);
+  if (nm == "gradth_x") return D(d.grad[4], np);
+  if (nm == "gradth_y") return D(d.grad[5], np);
+  if (nm == "gradC_x") return D(d.gradCx, n);
+  if (nm == "gradC_y") return D(d.gradCy, n);
+  if (nm == "ushift_x") return D(d.ushx, n);
+  if (nm == "ushift_y") return D(d.ushy, n);
+  if (nm == "ustar_x") return D(d.ux2, np);
+  if (nm == "ustar_y") return D(d.uy2, np);
+  if (nm == "theta_star") return D(d.th, n);
+  if (nm == "ppe_B") return D(d.ppe_B, n);
+  if (nm == "ppe_diag") return D(d.ppe_diag, n);
+  if (nm == "ppe_val") return D(d.ppe_val, ell);
+  if (nm == "ppe_col") return I(d.ppe_col, ell);
+  if (nm == "grad_px") return D(d.gpx, n);
+  if (nm == "grad_py") return D(d.gpy, n);
+  if (nm == "conc" && d.conc) return D(d.conc, n);
+  if (nm == "div_r" && d.div_r) return D(d.div_r, n);
+  return DView{nullptr, 0, -1};
+}
+
+int vebi_debug_size(vebi_ctx* h, const char* name, int64_t* esz, int64_t* count) {
+  if (!h || !name || !esz || !count) return fail(VEBI_ERR_ARG, "null argument");
+  cudaStreamSynchronize(h->x.st);
+  DView v = dview(h->x, name);
+  if (v.n < 0) return fail(VEBI_ERR_ARG, std::string("unknown field ") + name);
+  *esz = v.esz;
+  *count = v.n;
+  return VEBI_OK;
+}
+
+int vebi_debug_get(vebi_ctx* h, const char* name, void* out, int64_t bytes) {
+  if (!h || !name || !out) return fail(VEBI_ERR_ARG, "null argument");
+  cudaStreamSynchronize(h->x.st);
+  DView v = dview(h->x, name);
+  if (v.n < 0) return fail(VEBI_ERR_ARG, std::string("unknown field ") + name);
+  if (bytes < v.n * v.esz) return fail(VEBI_ERR_ARG, "buffer too small");
+  if (v.n > 0) CUDA_TRY(cudaMemcpy(out, v.p, (size_t)(v.n * v.esz), cudaMemcpyDeviceToHost));
+  return VEBI_OK;
+}
+
+}  // extern "C"

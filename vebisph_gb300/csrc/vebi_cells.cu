@@ -1,0 +1,226 @@
+// vebi_cells.cu -- cell binning and the neighbour (pair) list.
+//
+//  divide                      neighbour_finding_mod.F90:56-127
+//  neighboring_list_parallel   neighbour_finding_mod.F90:261-339
+//  neighbour_particle_cell     neighbour_finding_mod.F90:341-365
+//
+// Binning is a counting sort on the reference's dense cell keys ii = icell + (jcell-1)*ncx
+// (a one-digit radix sort): atomic counts, an exclusive scan, an atomic scatter, and a
+// warp-per-cell sort that restores the reference's stable order (ascending particle index
+// inside a cell).  The pair list is written in the ELL layout ij_link[k][i] (the Fortran
+// ij_link(npfb,nplink) array is already particle-fastest) in the reference's visiting
+// order C, E, NE, SE, W, NW, SW, N, S, so ij_link here equals ij_link of the reference.
+#include "vebi_ctx.cuh"
+
+namespace vebi {
+
+constexpr int SCAN_CH = 1024;  // cells per scan block
+
+__global__ void k_cell_key(Consts c, Dev d) {
+  const int np = d.s->np;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < np; k += gridDim.x * blockDim.x) {
+    int key = -1;
+    if (!d.inbin[k]) {
+      double ddx = d.rx[k] - c.x_mint, ddy = d.ry[k] - c.y_mint;
+      int icell = (int)(ddx * c.uno_sup_size) + 1;
+      int jcell = (int)(ddy * c.uno_sup_size) + 1;
+      long long ii = (long long)icell + (long long)(jcell - 1) * c.ncx;
+      // a NaN or huge coordinate converts to an out-of-range cell; never index with it
+      if (ii > c.nct || ii < 1 || !(ddx == ddx) || !(ddy == ddy)) {
+        set_error(d.s, VEBI_ERR_OUT_OF_DOMAIN);
+      } else {
+        key = (int)ii - 1;
+        int rank = atomicAdd(&d.cell_cnt[key], 1);
+        d.cell_fill[k] = rank;
+      }
+    }
+    d.cellpart[k] = key;
+  }
+}
+
+// exclusive scan of cell counts, pass 1: block totals; also the population bound
+__global__ void k_scan_blocks(Consts c, Dev d) {
+  __shared__ double sh[TPB / 32 + 1];
+  int b0 = blockIdx.x * SCAN_CH;
+  int loc = 0, mx = 0;
+  for (int q = threadIdx.x; q < SCAN_CH; q += blockDim.x) {
+    int cc = b0 + q;
+    if (cc < c.nct) {
+      int v = d.cell_cnt[cc];
+      loc += v;
+      mx = max(mx, v);
+    }
+  }
+  if (mx > c.nplink) set_error(d.s, VEBI_ERR_CELL_CAPACITY);
+  double t = block_sum<TPB>((double)loc, sh);
+  if (threadIdx.x == 0) d.scan_part[blockIdx.x] = (int)t;
+}
+
+// pass 2: exclusive scan of the block totals (one block)
+__global__ void k_scan_top(Dev d, int nblk) {
+  __shared__ int sh[1024];
+  const int T = blockDim.x;
+  int per = (nblk + T - 1) / T;
+  int b0 = threadIdx.x * per, b1 = min(nblk, b0 + per);
+  int loc = 0;
+  for (int b = b0; b < b1; ++b) loc += d.scan_part[b];
+  sh[threadIdx.x] = loc;
+  __syncthreads();
+  for (int o = 1; o < T; o <<= 1) {
+    int v = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+    __syncthreads();
+    sh[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int run = sh[threadIdx.x] - loc;
+  for (int b = b0; b < b1; ++b) {
+    int v = d.scan_part[b];
+    d.scan_part[b] = run;
+    run += v;
+  }
+}
+
+// pass 3: per-block exclusive scan plus block offset -> cell_start (ist)
+__global__ void k_scan_apply(Consts c, Dev d) {
+  __shared__ int sh[SCAN_CH];
+  __shared__ int wsum[32];
+  int b0 = blockIdx.x * SCAN_CH;
+  // each thread owns SCAN_CH/blockDim consecutive cells
+  const int per = SCAN_CH / TPB;
+  int vals[SCAN_CH / TPB];
+  int loc = 0;
+  for (int q = 0; q < per; ++q) {
+    int cc = b0 + threadIdx.x * per + q;
+    vals[q] = (cc < c.nct) ? d.cell_cnt[cc] : 0;
+    loc += vals[q];
+  }
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int inc = loc;
+  for (int o = 1; o < 32; o <<= 1) {
+    int v = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += v;
+  }
+  if (lane == 31) wsum[w] = inc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int q = 0; q < TPB / 32; ++q) { int v = wsum[q]; wsum[q] = run; run += v; }
+  }
+  __syncthreads();
+  int run = d.scan_part[blockIdx.x] + wsum[w] + inc - loc;
+  for (int q = 0; q < per; ++q) {
+    int cc = b0 + threadIdx.x * per + q;
+    if (cc < c.nct) d.cell_start[cc] = run;
+    run += vals[q];
+    if (cc == c.nct - 1) d.cell_start[c.nct] = run;
+  }
+  (void)sh;
+}
+
+__global__ void k_scatter(Dev d) {
+  const int np = d.s->np;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < np; k += gridDim.x * blockDim.x) {
+    int key = d.cellpart[k];
+    if (key >= 0) d.ip[d.cell_start[key] + d.cell_fill[k]] = k;
+  }
+}
+
+// warp per cell: restore ascending particle order inside each cell (the reference scatters
+// particles in ascending index, so each cell's list is sorted)
+__global__ void k_cell_sort(Consts c, Dev d) {
+  const int lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  const int nwarps = gridDim.x * wpb;
+  for (int cell = blockIdx.x * wpb + (threadIdx.x >> 5); cell < c.nct; cell += nwarps) {
+    int n = d.cell_cnt[cell];
+    if (n <= 1) continue;
+    if (n > 96) n = 96;  // capacity error already raised (nplink <= 96)
+    int s0 = d.cell_start[cell];
+    int v[3];
+    for (int q = 0; q < 3; ++q) {
+      int e = lane + 32 * q;
+      v[q] = e < n ? d.ip[s0 + e] : 0x7fffffff;
+    }
+    int rk[3] = {0, 0, 0};
+    for (int q2 = 0; q2 < 3; ++q2) {
+      if (32 * q2 >= n) break;
+      for (int src = 0; src < 32; ++src) {
+        int o = __shfl_sync(0xffffffffu, v[q2], src);
+        for (int q = 0; q < 3; ++q) rk[q] += (o < v[q]) ? 1 : 0;
+      }
+    }
+    __syncwarp();
+    for (int q = 0; q < 3; ++q) {
+      int e = lane + 32 * q;
+      if (e < n) d.ip[s0 + rk[q]] = v[q];
+    }
+    __syncwarp();
+  }
+}
+
+// pair list: thread per particle, cells in the reference's order, FP64 test 0 < r^2 <= 9h^2
+__global__ void k_neighbours(Consts c, Dev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.npfb) return;
+  int cnt = 0;
+  if (!d.inbin[i] && d.cellpart[i] >= 0) {
+    const double xi = d.rx[i], yi = d.ry[i];
+    const int ic = d.cellpart[i] + 1;  // 1-based as the reference
+    const int icx = ic % c.ncx;        // the reference's column formula: last column -> 0
+    const int icy = ic / c.ncx + 1;
+    int jcs[9];
+    int nj = 0;
+    jcs[nj++] = ic;
+    if (icx + 1 <= c.ncx) {
+      jcs[nj++] = ic + 1;
+      if (icy + 1 <= c.ncy) jcs[nj++] = ic + c.ncx + 1;
+      if (icy - 1 >= 1) jcs[nj++] = ic - c.ncx + 1;
+    }
+    if (icx - 1 >= 1) {
+      jcs[nj++] = ic - 1;
+      if (icy + 1 <= c.ncy) jcs[nj++] = ic + c.ncx - 1;
+      if (icy - 1 >= 1) jcs[nj++] = ic - c.ncx - 1;
+    }
+    if (icy + 1 <= c.ncy) jcs[nj++] = ic + c.ncx;
+    if (icy - 1 >= 1) jcs[nj++] = ic - c.ncx;
+    bool over = false;
+    for (int q = 0; q < nj; ++q) {
+      int jc = jcs[q];
+      if (jc < 1 || jc > c.nct) continue;  // cells past the grid are empty in the reference
+      int cc = jc - 1;
+      int s0 = d.cell_start[cc], s1 = s0 + d.cell_cnt[cc];
+      for (int jj = s0; jj < s1; ++jj) {
+        int j = d.ip[jj];
+        double r1 = xi - d.rx[j], r2 = yi - d.ry[j];
+        double rr2 = r1 * r1 + r2 * r2;
+        if (rr2 > 0.0 && rr2 <= c.sup_size_2) {
+          if (cnt < c.nplink) d.ij_link[(size_t)cnt * c.npfb + i] = j;
+          else over = true;
+          ++cnt;
+        }
+      }
+    }
+    if (over) {
+      set_error(d.s, VEBI_ERR_NEIGH_CAPACITY);
+      cnt = c.nplink;
+    }
+  }
+  d.ij_count[i] = cnt;
+  atomicMax(&d.s->maxneigh, cnt);
+}
+
+void launch_cells_neighbours(Ctx& x) {
+  const Consts& c = x.c;
+  cudaMemsetAsync(x.d.cell_cnt, 0, sizeof(int) * (size_t)c.nct, x.st);
+  VEBI_LAUNCH(x, k_cell_key, x.gs_blocks, TPB, c, x.d);
+  int nblk = (c.nct + SCAN_CH - 1) / SCAN_CH;
+  VEBI_LAUNCH(x, k_scan_blocks, nblk, TPB, c, x.d);
+  VEBI_LAUNCH(x, k_scan_top, 1, 1024, x.d, nblk);
+  VEBI_LAUNCH(x, k_scan_apply, nblk, TPB, c, x.d);
+  VEBI_LAUNCH(x, k_scatter, x.gs_blocks, TPB, x.d);
+  VEBI_LAUNCH(x, k_cell_sort, grid_for((long long)c.nct * 32), TPB, c, x.d);
+  stage_mark(x, 3);
+  VEBI_LAUNCH(x, k_neighbours, grid_for(c.npfb), TPB, c, x.d);
+}
+
+}  // namespace vebi

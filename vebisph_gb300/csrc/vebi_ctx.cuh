@@ -1,0 +1,56 @@
+// vebi_ctx.cuh -- host-side context of one simulation (opaque vebi_ctx of include/vebi.h).
+#pragma once
+
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "vebi_common.cuh"
+
+namespace vebi {
+
+struct Ctx {
+  vebi_params prm{};
+  Consts c{};
+  Dev d{};
+  cudaStream_t st = nullptr;
+  int device = 0;
+  int nsm = 0;
+  int launches = 0;
+  bool timing = false;
+  cudaEvent_t ev[VEBI_NSTAGES + 1]{};
+  bool ev_used[VEBI_NSTAGES]{};
+  int coop_blocks = 0;       // persistent PPE grid (co-resident blocks)
+  int gs_blocks = 0;         // grid of grid-stride kernels over dynamic counts
+  int sel_max_blocks = 0;    // blocks of the ordered-select kernels
+  int precision = VEBI_PREC_FP64;
+  bool have_state = false;
+  std::vector<void*> allocs;
+  vebi_step_stats last{};
+};
+
+// kernel launch with launch accounting and an immediate launch-error check
+#define VEBI_LAUNCH(x, kern, grid, block, ...)                         \
+  do {                                                                 \
+    kern<<<(grid), (block), 0, (x).st>>>(__VA_ARGS__);                 \
+    (x).launches++;                                                    \
+  } while (0)
+
+inline int grid_for(long long n, int tpb = TPB) {
+  long long g = (n + tpb - 1) / tpb;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+// stage timers: record the start event of stage `s` (ends at the next recorded stage)
+inline void stage_mark(Ctx& x, int s) {
+  if (!x.timing) return;
+  cudaEventRecord(x.ev[s], x.st);
+  x.ev_used[s] = true;
+}
+
+// ordered-select items per block
+constexpr int SEL_IPT = 8;
+constexpr int SEL_CH = TPB * SEL_IPT;
+
+}  // namespace vebi

@@ -1,0 +1,383 @@
+// vebi_ppe.cu -- pressure Poisson equation: right-hand side, assembly and BiCGSTAB.
+//
+//  ppe_solve_in_house_simple_dirichlet   ppe_solve_in_house_simple_dirichlet.F90:1-158
+//  SPARSE_PBICGSTAB_nonull (closed)       linear_solver.F90:275-425
+//  SPARSE_PBICGSTAB (open, Jacobi)        linear_solver.F90:82-227
+//  sparse_atime, vtime, norm, remove_dc, inverseM
+//
+// Matrix layout.  The reference stores the Laplacian in Numerical Recipes row-indexed form:
+// A(1:n) the diagonal, then one off-diagonal slot per neighbour of each row, in neighbour
+// order (ppe...:60-121).  Here the same slots live in ELL form, ppe_col/ppe_val[k][i],
+// k < ij_count(i), beside ppe_diag[i]; slot k of row i is NR slot ia(i)+k-1.  A mirror
+// neighbour maps to its parent's column; duplicate columns accumulate into the last slot
+// written for that column and leave 0 in the earlier ones, as the reference does.
+//
+// Solver.  One persistent cooperative kernel runs the whole BiCGSTAB loop.  Every global
+// reduction is a block partial written to `partials` followed by a bounded grid barrier, after
+// which every block sums the partials in the same fixed order, so all blocks hold identical
+// scalars and take identical branches.  Seven barriers per iteration (closed domain):
+//   p-update+sum(p) | p-=mean, p_inv | v=A p_inv, (r_bar,v) | s, |s|^2, sum(s) |
+//   s-=mean, s_inv | t=A s_inv, (t,s), |t|^2 | x,r update, |r|^2, (r_bar,r)
+// The barrier spins are bounded: on timeout the kernel records VEBI_ERR_TIMEOUT and returns.
+#include "vebi_ctx.cuh"
+
+namespace vebi {
+
+#define ELL(k, i) ((size_t)(k) * c.npfb + (i))
+
+// ---------------------------------------------------------------------- right-hand side
+__global__ void k_ppe_rhs(Consts c, Dev d) {
+  __shared__ double sh[TPB / 32 + 1];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double b = 0.0;
+  if (i < c.npfb) {
+    const double ui = d.ux[i], vi = d.uy[i];
+    const double K11 = d.kgcm[0][i], K21 = d.kgcm[1][i], K12 = d.kgcm[2][i], K22 = d.kgcm[3][i];
+    double fb = 0.0;
+    const int cnt = d.ij_count[i];
+    for (int k = 0; k < cnt; ++k) {
+      int j = d.ij_link[ELL(k, i)];
+      double u1 = ui - d.ux[j], u2 = vi - d.uy[j];
+      double w1 = d.wGx[ELL(k, i)], w2 = d.wGy[ELL(k, i)];
+      double kw1 = K11 * w1 + K12 * w2, kw2 = K21 * w1 + K22 * w2;
+      fb = fb - (u1 * kw1 + u2 * kw2);
+    }
+    b = fb / d.s->dt;
+    d.ppe_B[i] = b;
+  }
+  double bs = block_sum<TPB>(b, sh);
+  if (threadIdx.x == 0) d.partials[blockIdx.x] = bs;
+}
+
+__global__ void k_ppe_mean(Consts c, Dev d, int nblk) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s = 0.0;
+  for (int b = 0; b < nblk; ++b) s += d.partials[b];
+  d.s->rhs_mean = (c.open_domain == 0) ? s / (double)c.npfb : 0.0;
+}
+
+// ---------------------------------------------------------------------- assembly
+__global__ void k_ppe_assemble(Consts c, Dev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.npfb) return;
+  double B = d.ppe_B[i];
+  if (c.open_domain == 0) B = B - d.s->rhs_mean;
+  const int cnt = d.ij_count[i];
+  bool any_mirror = false;
+  for (int k = 0; k < cnt; ++k) {
+    int j = d.ij_link[ELL(k, i)];
+    int col = j;
+    if (j >= c.npfb) { col = d.irel[j]; any_mirror = true; }
+    d.ppe_col[ELL(k, i)] = col;
+    d.ppe_val[ELL(k, i)] = 0.0;
+  }
+  double Adiag = 0.0;
+  for (int k = 0; k < cnt; ++k) {
+    int j = d.ij_link[ELL(k, i)];
+    double temp = -d.wL[ELL(k, i)];
+    Adiag = Adiag - temp;
+    int colk = j;
+    bool self = false;
+    if (j >= c.npfb) {
+      colk = d.irel[j];
+      if (colk == i) self = true;
+      B = B - d.dP_mp[j] * temp;
+    }
+    if (self) {
+      Adiag = Adiag + temp;
+    } else {
+      int nt = k;  // last slot holding this column
+      if (any_mirror) {
+        for (int kk = cnt - 1; kk >= 0; --kk)
+          if (d.ppe_col[ELL(kk, i)] == colk) { nt = kk; break; }
+      }
+      d.ppe_val[ELL(nt, i)] = d.ppe_val[ELL(nt, i)] + temp;
+    }
+  }
+  if (d.n_surf[i] != 0) Adiag = 1.0e30;
+  d.ppe_diag[i] = 0.0 + Adiag;
+  if (c.open_domain == 1 && d.n_surf[i] != 1 && d.ppe_smooth[i] != 1.0) {
+    const double ps = d.ppe_smooth[i];
+    B = B * ps;
+    for (int k = 0; k < cnt; ++k) d.ppe_val[ELL(k, i)] = d.ppe_val[ELL(k, i)] * ps;
+  }
+  d.ppe_B[i] = B;
+}
+
+// ---------------------------------------------------------------------- BiCGSTAB
+constexpr unsigned long long SPIN_LIMIT = 1ull << 25;  // ~2-4 s of __nanosleep(64) polls
+
+// bounded grid-wide barrier for a co-resident (cooperative) grid; false on error/timeout
+__device__ __forceinline__ bool grid_sync(Scal* s) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* vgen = &s->bar_gen;
+    volatile int* verr = &s->error;
+    unsigned int g = *vgen;
+    __threadfence();
+    unsigned int arrived = atomicAdd((unsigned int*)&s->bar_count, 1u) + 1u;
+    if (arrived == gridDim.x) {
+      atomicExch((unsigned int*)&s->bar_count, 0u);
+      __threadfence();
+      atomicAdd((unsigned int*)&s->bar_gen, 1u);
+    } else {
+      unsigned long long spins = 0;
+      while (*vgen == g) {
+        if (*verr != 0) break;
+        if (++spins > SPIN_LIMIT) {
+          atomicCAS((int*)&s->error, 0, VEBI_ERR_TIMEOUT);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *((volatile int*)&s->error) == 0;
+}
+
+// sum of the block partials of `slot` in a fixed order; identical in every block
+__device__ __forceinline__ void reduce_partials(const double* part, int nb, int nval, double* out,
+                                                double* shv) {
+  if (threadIdx.x < 32) {
+    for (int q = 0; q < nval; ++q) {
+      double v = 0.0;
+      for (int b = threadIdx.x; b < nb; b += 32) v += __ldcg(part + (size_t)q * nb + b);
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (threadIdx.x == 0) shv[q] = v;
+    }
+  }
+  __syncthreads();
+  for (int q = 0; q < nval; ++q) out[q] = shv[q];
+  __syncthreads();
+}
+
+// block partial of one or two values into part[q*nb + blockIdx.x]
+__device__ __forceinline__ void write_partials(double a, double b, int nval, double* part, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) { sh[w] = a; sh[32 + w] = b; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sa = 0.0, sb = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { sa += sh[q]; sb += sh[32 + q]; }
+    part[blockIdx.x] = sa;
+    if (nval > 1) part[gridDim.x + blockIdx.x] = sb;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ double spmv_row(const Consts& c, const int* __restrict__ cnt_,
+                                           const double* __restrict__ diag, const double* __restrict__ val,
+                                           const int* __restrict__ col, const double* xv, int i) {
+  double bb = __ldg(diag + i) * __ldcg(xv + i);
+  const int cnt = __ldg(cnt_ + i);
+  for (int k = 0; k < cnt; ++k) {
+    size_t e = ELL(k, i);
+    bb = fma(__ldg(val + e), __ldcg(xv + __ldg(col + e)), bb);
+  }
+  return bb;
+}
+
+template <bool NONULL>
+__global__ void __launch_bounds__(TPB) k_bicgstab(Consts c, Dev d) {
+  __shared__ double sh[64];
+  __shared__ double shv[4];
+  const int n = c.npfb;
+  const int nb = gridDim.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int stride = gridDim.x * blockDim.x;
+  Scal* s = d.s;
+  double* part = d.partials;
+  double* __restrict__ x = d.bx;
+  double* __restrict__ r = d.br;
+  double* __restrict__ rb = d.brb;
+  double* __restrict__ v = d.bv;
+  double* __restrict__ p = d.bp;
+  double* __restrict__ pinv = d.bpi;
+  double* __restrict__ sv = d.bs;
+  double* __restrict__ sinv = d.bsi;
+  double* __restrict__ t = d.bt;
+  const double* __restrict__ Bv = d.ppe_B;
+  const double* __restrict__ diag = d.ppe_diag;
+  const double* __restrict__ val = d.ppe_val;
+  const int* __restrict__ col = d.ppe_col;
+  const int* __restrict__ cnt = d.ij_count;
+  const double tol = c.tol;
+  const double small = NONULL ? 1.0e-6 : 4.0;  // open solver: the integer expression 10-6
+  // M: 1 (closed) or the diagonal (open); inverseM divides by M+1e-15
+  auto minv_den = [&](int i) -> double { return NONULL ? (1.0 + 1.0e-15) : (__ldg(diag + i) + 1.0e-15); };
+  double red[2];
+  // initial guess x = 0: r = B - A*0 = B
+  double acc = 0.0;
+  for (int i = tid; i < n; i += stride) {
+    double bi = Bv[i];
+    x[i] = 0.0;
+    r[i] = bi;
+    rb[i] = bi;
+    v[i] = 0.0;
+    p[i] = 0.0;
+    acc += bi * bi;
+  }
+  // slot 10 for the initial reduction: slot 0 is rewritten before every block has read it
+  write_partials(acc, 0.0, 1, part + 10 * (size_t)nb, sh);
+  if (!grid_sync(s)) return;
+  reduce_partials(part + 10 * (size_t)nb, nb, 1, red, shv);
+  double rho = red[0], rho0 = 1.0, alpha = 1.0, omega = 1.0;
+  double n2r0 = 1.0, n2s0 = 1.0, resid = 0.0;
+  int iter = 1, warn = 0;
+  bool done = false;
+  while (iter <= c.itermax) {
+    if (rho == 0.0) { warn |= VEBI_WARN_BICGSTAB_BREAKDOWN; done = true; break; }
+    // p = r + beta (p - omega v)
+    double beta = rho / (rho0 + 1.0e-15) * alpha / (omega + 1.0e-15);
+    acc = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      double pi = (iter == 1) ? r[i] : r[i] + beta * (p[i] - omega * v[i]);
+      p[i] = pi;
+      acc += pi;
+    }
+    double* slot = part + 0 * (size_t)nb;
+    if (NONULL) {
+      write_partials(acc, 0.0, 1, slot, sh);
+      if (!grid_sync(s)) return;
+      reduce_partials(slot, nb, 1, red, shv);
+      const double mean = red[0] / (double)n;
+      for (int i = tid; i < n; i += stride) {
+        double pi = p[i] - mean;
+        p[i] = pi;
+        pinv[i] = pi / minv_den(i);
+      }
+    } else {
+      for (int i = tid; i < n; i += stride) pinv[i] = p[i] / minv_den(i);
+    }
+    if (!grid_sync(s)) return;
+    // v = A p_inv ; (r_bar, v)
+    acc = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      double vi = spmv_row(c, cnt, diag, val, col, pinv, i);
+      v[i] = vi;
+      acc += rb[i] * vi;
+    }
+    slot = part + 2 * (size_t)nb;
+    write_partials(acc, 0.0, 1, slot, sh);
+    if (!grid_sync(s)) return;
+    reduce_partials(slot, nb, 1, red, shv);
+    alpha = rho / (red[0] + 1.0e-15);
+    // s = r - alpha v ; |s|^2 ; sum(s)
+    double a2 = 0.0;
+    acc = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      double si = r[i] - alpha * v[i];
+      sv[i] = si;
+      acc += si * si;
+      a2 += si;
+    }
+    slot = part + 4 * (size_t)nb;
+    write_partials(acc, a2, 2, slot, sh);
+    if (!grid_sync(s)) return;
+    reduce_partials(slot, nb, 2, red, shv);
+    const double n2s = red[0];
+    const double mean_s = red[1] / (double)n;
+    if (iter == 1) n2s0 = (n2s <= small) ? 1.0 : n2s;
+    if (n2s <= tol * tol * n2s0) {
+      for (int i = tid; i < n; i += stride) x[i] = x[i] + alpha * pinv[i];
+      resid = sqrt(n2s / n2s0);
+      done = true;
+      break;
+    }
+    // s -= mean (closed) ; s_inv
+    for (int i = tid; i < n; i += stride) {
+      double si = sv[i];
+      if (NONULL) { si = si - mean_s; sv[i] = si; }
+      sinv[i] = si / minv_den(i);
+    }
+    if (!grid_sync(s)) return;
+    // t = A s_inv ; (t, s) ; |t|^2
+    acc = 0.0;
+    a2 = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      double ti = spmv_row(c, cnt, diag, val, col, sinv, i);
+      t[i] = ti;
+      acc += ti * sv[i];
+      a2 += ti * ti;
+    }
+    slot = part + 6 * (size_t)nb;
+    write_partials(acc, a2, 2, slot, sh);
+    if (!grid_sync(s)) return;
+    reduce_partials(slot, nb, 2, red, shv);
+    omega = red[0] / (red[1] + 1.0e-15);
+    // x, r update ; |r|^2 ; (r_bar, r) for the next rho
+    acc = 0.0;
+    a2 = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      x[i] = x[i] + alpha * pinv[i] + omega * sinv[i];
+      double ri = sv[i] - omega * t[i];
+      r[i] = ri;
+      acc += ri * ri;
+      a2 += rb[i] * ri;
+    }
+    slot = part + 8 * (size_t)nb;
+    write_partials(acc, a2, 2, slot, sh);
+    if (!grid_sync(s)) return;
+    reduce_partials(slot, nb, 2, red, shv);
+    const double n2r = red[0];
+    if (iter == 1) n2r0 = (n2r <= small) ? 1.0 : n2r;
+    resid = sqrt(n2r / n2r0);
+    if (n2r <= tol * tol * n2r0) { done = true; break; }
+    iter = iter + 1;
+    rho0 = rho;
+    rho = red[1];
+  }
+  if (!done) warn |= VEBI_WARN_MAXITER;
+  for (int i = tid; i < n; i += stride) d.p[i] = x[i];
+  if (tid == 0) {
+    s->ls_iters = iter;
+    s->ls_residual = resid;
+    atomicOr(&s->warnings, warn);
+  }
+}
+
+int ppe_solver_blocks(int device, int nsm) {
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_bicgstab<true>, TPB, 0);
+  int per2 = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, k_bicgstab<false>, TPB, 0);
+  per = per < per2 ? per : per2;
+  if (per < 1) per = 1;
+  (void)device;
+  return per * nsm;
+}
+
+void launch_ppe(Ctx& x) {
+  const Consts& c = x.c;
+  int g = grid_for(c.npfb);
+  stage_mark(x, 9);
+  VEBI_LAUNCH(x, k_ppe_rhs, g, TPB, c, x.d);
+  VEBI_LAUNCH(x, k_ppe_mean, 1, 32, c, x.d, g);
+  VEBI_LAUNCH(x, k_ppe_assemble, g, TPB, c, x.d);
+  stage_mark(x, 10);
+  // persistent cooperative launch: all blocks co-resident, so the grid barrier is safe
+  int nblk = x.coop_blocks;
+  long long need = (c.npfb + TPB - 1) / TPB;
+  if (need < nblk) nblk = (int)(need < 1 ? 1 : need);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nblk);
+  cfg.blockDim = dim3(TPB);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = x.st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (c.open_domain == 0) cudaLaunchKernelEx(&cfg, k_bicgstab<true>, c, x.d);
+  else cudaLaunchKernelEx(&cfg, k_bicgstab<false>, c, x.d);
+  x.launches++;
+}
+
+}  // namespace vebi

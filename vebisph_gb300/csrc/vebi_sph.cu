@@ -1,0 +1,469 @@
+// vebi_sph.cu -- per-pair SPH operators and per-particle updates of the step.
+//
+//  kernel_calculation (weights, Bonet-Lok kgcm)   kernel_calculation.F90:2-75
+//  locate_free_surf_part, calc_part_dist_vars,
+//  smooth_normals (open domain)                   freesurf_mod.F90:17-137
+//  new_fick_shift + shifting_forces               new_fick_shift.F90:15-92,117-210
+//  grad_operator (u, v, theta in one pass)        gradient_calculation.F90:50-94
+//  constitutive_eqn_evolve, calc_eigens,
+//  f_strain_*, f_relaxation_integrate             predictor_mod.F90:141-331
+//  prediction_step pair loop and updates          predictor_mod.F90:27-139
+//  calc_pressure_gradient + velocity update +
+//  final advection                                gradient_calculation.F90:16-48, div_free.F90:94-117
+//  secondary_properties                           div_free.F90:148-192
+//
+// One thread per particle walks that particle's ELL row k = 0..ij_count-1 in the reference's
+// order with the reference's association, so every per-particle sum is the reference's sum.
+#include "vebi_ctx.cuh"
+
+namespace vebi {
+
+#define ELL(k, i) ((size_t)(k) * c.npfb + (i))
+
+// ---------------------------------------------------------------------- kernel_calculation
+__global__ void k_weights(Consts c, Dev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.npfb) return;
+  const double xi = d.rx[i], yi = d.ry[i], dv = c.dv;
+  double k11 = 0.0, k12 = 0.0, k21 = 0.0, k22 = 0.0;
+  const int cnt = d.ij_count[i];
+  for (int k = 0; k < cnt; ++k) {
+    int j = d.ij_link[ELL(k, i)];
+    double r1 = xi - d.rx[j], r2 = yi - d.ry[j];
+    double rr2 = r1 * r1 + r2 * r2;
+    double rad = sqrt(rr2);
+    double qq = rad * c.oneoverh;
+    double f = fac(c, qq);
+    double m = fmax(rad, c.eta2);
+    double g1 = r1 * f / m, g2 = r2 * f / m;
+    double w1 = g1 * dv, w2 = g2 * dv;
+    d.wGx[ELL(k, i)] = w1;
+    d.wGy[ELL(k, i)] = w2;
+    d.wL[ELL(k, i)] = 2.0 * (r1 * w1 + r2 * w2) / (rr2 + c.eta_small);
+    k11 = k11 - dv * g1 * r1;
+    k12 = k12 - dv * g2 * r1;
+    k21 = k21 - dv * g1 * r2;
+    k22 = k22 - dv * g2 * r2;
+  }
+  double temp = 1.0 / ((k11 * k22 - k12 * k21) + 1.0e-15);
+  d.kgcm[0][i] = temp * k22;
+  d.kgcm[2][i] = -temp * k12;
+  d.kgcm[1][i] = -temp * k21;
+  d.kgcm[3][i] = temp * k11;
+}
+
+// ---------------------------------------------------------------------- free surface (open)
+__global__ void k_part_dist_vars(Consts c, Dev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.npfb) return;
+  const double xi = d.rx[i], yi = d.ry[i];
+  double ct = 0, dr = 0, s1 = 0, s2 = 0;
+  const int cnt = d.ij_count[i];
+  for (int k = 0; k < cnt; ++k) {
+    int j = d.ij_link[ELL(k, i)];
+    double r1 = xi - d.rx[j], r2 = yi - d.ry[j];
+    double rad = sqrt(r1 * r1 + r2 * r2);
+    ct = ct + wab(c, rad / c.h);
+    double w1 = d.wGx[ELL(k, i)], w2 = d.wGy[ELL(k, i)];
+    dr = dr - (r1 * w1 + r2 * w2);
+    s1 = s1 - w1;
+    s2 = s2 - w2;
+  }
+  double w0 = wab(c, 0.0);
+  double conc = ct * c.dv;
+  conc = conc + c.dv * w0;
+  d.conc[i] = conc;
+  d.div_r[i] = dr;
+  d.surf_nx[i] = s1 * c.h;
+  d.surf_ny[i] = s2 * c.h;
+  double bdr = 1.4 + 0.5 * fmax(conc - 1.0, -0.2);
+  d.beta_div_r[i] = bdr;
+  d.n_surf[i] = (dr > bdr) ? 0 : 1;
+}
+
+__global__ void k_nsurf_mirrors(Consts c, Dev d) {
+  const int nm = d.s->nmirror;
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nm; m += gridDim.x * blockDim.x) {
+    int j = c.npfb + m;
+    d.n_surf[j] = d.n_surf[d.irel[j]];
+  }
+}
+
+// smooth_normals (Shepard filter) + ppe_smooth; the filtered normals go to gradCx/gradCy
+// scratch first and are copied back after (the reference uses a temporary array too)
+__global__ void k_smooth_normals(Consts c, Dev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.npfb) return;
+  const double xi = d.rx[i], yi = d.ry[i];
+  double a = 0, b = 0;
+  const int cnt = d.ij_count[i];
+  for (int k = 0; k < cnt; ++k) {
+    int j = d.ij_link[ELL(k, i)];
+    if (j >= c.npfb) continue;
+    double r1 = xi - d.rx[j], r2 = yi - d.ry[j];
+    double rad = sqrt(r1 * r1 + r2 * r2);
+    double w = wab(c, rad / c.h);
+    a = a + w * d.surf_nx[j];
+    b = b + w * d.surf_ny[j];
+  }
+  double w0 = wab(c, 0.0);
+  d.gradCx[i] = a * c.dv + d.surf_nx[i] * w0 * c.dv;
+  d.gradCy[i] = b * c.dv + d.surf_ny[i] * w0 * c.dv;
+  double ps = 1.0;
+  double dr = d.div_r[i], bdr = d.beta_div_r[i];
+  if (!(dr > 1.2 * bdr)) {
+    if (d.n_surf[i] == 1) ps = 0.0;
+    else ps = 0.5 * (1.0 - cos((dr - bdr) * PI / (0.2 * bdr)));
+  }
+  d.ppe_smooth[i] = ps;
+}
+
+__global__ void k_copy_normals(Consts c, Dev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.npfb) return;
+  d.surf_nx[i] = d.gradCx[i];
+  d.surf_ny[i] = d.gradCy[i];
+}
+
+// ---------------------------------------------------------------------- shifting
+__global__ void k_shift(Consts c, Dev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.npfb) return;
+  const double xi = d.rx[i], yi = d.ry[i];
+  double f1 = 0, f2 = 0, t1 = 0, t2 = 0;
+  const int cnt = d.ij_count[i];
+  for (int k = 0; k < cnt; ++k) {
+    int j = d.ij_link[ELL(k, i)];
+    double r1 = xi - d.rx[j], r2 = yi - d.ry[j];
+    double rad = sqrt(r1 * r1 + r2 * r2);
+    double qq = rad / c.h;
+    // Rt*(Wab/Wab1)**nt with nt = 4.0 (new_fick_shift.F90:135-148); the reference calls pow
+    double fab = 0.25 * pw4(wab(c, qq) / c.wab1);
+    double w1 = d.wGx[ELL(k, i)], w2 = d.wGy[ELL(k, i)];
+    f1 = f1 + w1;
+    f2 = f2 + w2;
+    t1 = t1 + w1 * fab;
+    t2 = t2 + w2 * fab;
+  }
+  double gx = f1 + t1, gy = f2 + t2;
+  d.gradCx[i] = gx;
+  d.gradCy[i] = gy;
+  const double dt = d.s->dt;
+  double d1 = 0.0, d2 = 0.0;
+  if (i >= c.nbS) {
+    double D;
+    if (c.shift_coeff == 1) {
+      double maxU = bits_to_double(d.s->maxU_bits);
+      double absU = sqrt(d.ux[i] * d.ux[i] + d.uy[i] * d.uy[i]);
+      double temp = (double)0.2f * exp(-absU / ((double)0.2f * maxU));
+      D = 4.0 * c.h * dt * (absU + temp * maxU);
+    } else {
+      D = 0.25 * c.h * c.h;
+    }
+    if (d.n_surf[i] == 1 && c.open_domain == 1) {
+      double temp = sqrt(d.surf_nx[i] * d.surf_nx[i] + d.surf_ny[i] * d.surf_ny[i]);
+      double sn1 = d.surf_nx[i] / fmax(temp, (double)1e-8f);
+      double sn2 = d.surf_ny[i] / fmax(temp, (double)1e-8f);
+      double st1 = -sn2, st2 = sn1;
+      double dCds = st1 * gx + st2 * gy;
+      d1 = -D * dCds * st1;
+      d2 = -D * dCds * st2;
+    } else {
+      d1 = -D * gx;
+      d2 = -D * gy;
+    }
+    double temp = sqrt(d1 * d1 + d2 * d2);
+    if (temp > 0.1 * c.h) {
+      d1 = 0.1 * c.h * d1 / temp;
+      d2 = 0.1 * c.h * d2 / temp;
+    }
+  }
+  // ushift = dr_fs/dt; solid boundary particles get -u (div_free.F90:65-78)
+  if (i < c.nbS) {
+    d.ushx[i] = -d.ux[i];
+    d.ushy[i] = -d.uy[i];
+  } else {
+    d.ushx[i] = d1 / dt;
+    d.ushy[i] = d2 / dt;
+  }
+}
+
+// ---------------------------------------------------------------------- gradients
+__global__ void k_gradients(Consts c, Dev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.npfb) return;
+  const double ui = d.ux[i], vi = d.uy[i], ti = d.th[i];
+  double a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0;
+  const int cnt = d.ij_count[i];
+  for (int k = 0; k < cnt; ++k) {
+    int j = d.ij_link[ELL(k, i)];
+    double w1 = d.wGx[ELL(k, i)], w2 = d.wGy[ELL(k, i)];
+    double du = d.ux[j] - ui, dvv = d.uy[j] - vi, dth = d.th[j] - ti;
+    a0 = a0 + du * w1;
+    a1 = a1 + du * w2;
+    a2 = a2 + dvv * w1;
+    a3 = a3 + dvv * w2;
+    a4 = a4 + dth * w1;
+    a5 = a5 + dth * w2;
+  }
+  const double K11 = d.kgcm[0][i], K21 = d.kgcm[1][i], K12 = d.kgcm[2][i], K22 = d.kgcm[3][i];
+  d.grad[0][i] = K11 * a0 + K12 * a1;
+  d.grad[1][i] = K21 * a0 + K22 * a1;
+  d.grad[2][i] = K11 * a2 + K12 * a3;
+  d.grad[3][i] = K21 * a2 + K22 * a3;
+  d.grad[4][i] = K11 * a4 + K12 * a5;
+  d.grad[5][i] = K21 * a4 + K22 * a5;
+}
+
+// ---------------------------------------------------------------------- log-conformation
+struct M2 { double a11, a12, a21, a22; };
+__device__ __forceinline__ M2 mm(const M2& A, const M2& B) {
+  return M2{A.a11 * B.a11 + A.a12 * B.a21, A.a11 * B.a12 + A.a12 * B.a22,
+            A.a21 * B.a11 + A.a22 * B.a21, A.a21 * B.a12 + A.a22 * B.a22};
+}
+__device__ __forceinline__ M2 tr(const M2& A) { return M2{A.a11, A.a21, A.a12, A.a22}; }
+
+// calc_eigens (predictor_mod.F90:253-290): closed-form symmetric 2x2 eigen-decomposition
+__device__ __forceinline__ void calc_eigens(const M2& A, double& L1, double& L2, M2& R) {
+  double trc = A.a11 + A.a22;
+  double det = A.a11 * A.a22 - A.a21 * A.a12;
+  double tmp = 0.25 * trc * trc - det;
+  if (tmp <= 2.220446049250313e-16) tmp = 0.0;  // epsilon(1d0)
+  L1 = 0.5 * trc + sqrt(tmp);
+  L2 = 0.5 * trc - sqrt(tmp);
+  if (A.a21 != 0.0) {
+    double r11 = L1 - A.a22, r21 = A.a21;
+    double nrm = sqrt(r11 * r11 + r21 * r21);
+    r11 = r11 / nrm;
+    r21 = r21 / nrm;
+    R = M2{r11, -r21, r21, r11};
+  } else {
+    L1 = A.a11;
+    L2 = A.a22;
+    R = M2{1.0, 0.0, 0.0, 1.0};
+  }
+}
+
+__global__ void k_logconf(Consts c, Dev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.npfb) return;
+  const double dt = d.s->dt;
+  // steps 1-2: A = f_strain_backward(tau) = (tau/1 + I)/1
+  M2 A{d.tau[0][i] / 1.0 + 1.0, d.tau[2][i] / 1.0 + 0.0, d.tau[1][i] / 1.0 + 0.0, d.tau[3][i] / 1.0 + 1.0};
+  A = M2{A.a11 / 1.0, A.a12 / 1.0, A.a21 / 1.0, A.a22 / 1.0};
+  double L1, L2;
+  M2 R;
+  calc_eigens(A, L1, L2, R);
+  // step 3: Psi = R log(Lambda) R^T
+  M2 D{log(L1), 0.0, 0.0, log(L2)};
+  M2 Psi0 = mm(R, mm(D, tr(R)));
+  // step 5: B and Omega from R^T grad(u) R
+  M2 G{d.grad[0][i], d.grad[1][i], d.grad[2][i], d.grad[3][i]};
+  M2 tm = mm(tr(R), mm(G, R));
+  double tmp1 = (L2 * tm.a12 + L1 * tm.a21) / (L2 - L1 + 1e-10);
+  tm.a12 = 0.0;
+  tm.a21 = 0.0;
+  M2 B = mm(R, mm(tm, tr(R)));
+  M2 W{0.0, tmp1, -tmp1, 0.0};
+  M2 Om = mm(R, mm(W, tr(R)));
+  // step 6: Psi += dt (2B + Omega Psi - Psi Omega)
+  M2 OP = mm(Om, Psi0), PO = mm(Psi0, Om);
+  M2 t6{2.0 * B.a11 + OP.a11 - PO.a11, 2.0 * B.a12 + OP.a12 - PO.a12, 2.0 * B.a21 + OP.a21 - PO.a21,
+        2.0 * B.a22 + OP.a22 - PO.a22};
+  M2 Psi{Psi0.a11 + dt * t6.a11, Psi0.a12 + dt * t6.a12, Psi0.a21 + dt * t6.a21, Psi0.a22 + dt * t6.a22};
+  // step 7: A = R exp(Lambda) R^T
+  calc_eigens(Psi, L1, L2, R);
+  L1 = exp(L1);
+  L2 = exp(L2);
+  M2 E2{L1, 0.0, 0.0, L2};
+  A = mm(R, mm(E2, tr(R)));
+  // step 8: analytic PTT relaxation with the previous trace
+  double alpha_R = 1.0 + c.eps_ptt * (d.trace_conf[i] - 2.0);
+  double e1 = exp(-(alpha_R * 1.0 * dt / c.Wi));
+  double e2 = (1.0 - e1) / 1.0;
+  A = M2{A.a11 * e1 + e2 * 1.0, A.a12 * e1 + e2 * 0.0, A.a21 * e1 + e2 * 0.0, A.a22 * e1 + e2 * 1.0};
+  // step 9
+  double trc = A.a11 + A.a22;
+  d.trace_conf[i] = trc;
+  d.a_out[i] = trc;
+  d.tau[0][i] = 1.0 * (1.0 * A.a11 - 1.0);
+  d.tau[2][i] = 1.0 * (1.0 * A.a12 - 0.0);
+  d.tau[1][i] = 1.0 * (1.0 * A.a21 - 0.0);
+  d.tau[3][i] = 1.0 * (1.0 * A.a22 - 1.0);
+}
+
+// ---------------------------------------------------------------------- predictor
+// rhs pair loop + buoyancy; u*, theta* written to the second buffers (walls copied)
+__global__ void k_predictor(Consts c, Dev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.npfb) return;
+  const double ui = d.ux[i], vi = d.uy[i], ti = d.th[i];
+  const double K11 = d.kgcm[0][i], K21 = d.kgcm[1][i], K12 = d.kgcm[2][i], K22 = d.kgcm[3][i];
+  double Ti11 = 0, Ti21 = 0, Ti12 = 0, Ti22 = 0;
+  const bool ve = c.const_mod != 1;
+  if (ve) { Ti11 = d.tau[0][i]; Ti21 = d.tau[1][i]; Ti12 = d.tau[2][i]; Ti22 = d.tau[3][i]; }
+  const double cs = c.coeff_solvent, cp = c.coeff_polymeric, ct = c.coeff_theta;
+  double s1 = 0, s2 = 0, st = 0;
+  const int cnt = d.ij_count[i];
+  for (int k = 0; k < cnt; ++k) {
+    int j = d.ij_link[ELL(k, i)];
+    double u1 = ui - d.ux[j], u2 = vi - d.uy[j];
+    double wl = d.wL[ELL(k, i)];
+    if (ve) {
+      double w1 = d.wGx[ELL(k, i)], w2 = d.wGy[ELL(k, i)];
+      double T11 = d.tau[0][j] - Ti11, T21 = d.tau[1][j] - Ti21;
+      double T12 = d.tau[2][j] - Ti12, T22 = d.tau[3][j] - Ti22;
+      double kw1 = K11 * w1 + K12 * w2, kw2 = K21 * w1 + K22 * w2;
+      double tw1 = T11 * kw1 + T12 * kw2, tw2 = T21 * kw1 + T22 * kw2;
+      s1 = s1 + cp * tw1 + cs * u1 * wl;
+      s2 = s2 + cp * tw2 + cs * u2 * wl;
+    } else {
+      s1 = s1 + cs * u1 * wl;
+      s2 = s2 + cs * u2 * wl;
+    }
+    double thij = ti - d.th[j];
+    st = st + ct * thij * wl;
+  }
+  s2 = s2 + ti;  // buoyancy (predictor_mod.F90:111-119)
+  const double dt = d.s->dt;
+  if (i >= c.nbS) {
+    d.ux2[i] = ui + s1 * dt;
+    d.uy2[i] = vi + s2 * dt;
+    d.th2[i] = ti + st * dt;
+  } else {
+    d.ux2[i] = ui;
+    d.uy2[i] = vi;
+    d.th2[i] = ti;
+  }
+}
+
+// ---------------------------------------------------------------------- pressure gradient
+// grad P, velocity update (div_free.F90:96-101), final advection (:111-117); reads the
+// current buffers (u*) and writes u^{n+1}, r^{n+1} into the second buffers.
+__global__ void k_pgrad_final(Consts c, Dev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.npfb) return;
+  const double pi_ = d.p[i];
+  double a = 0, b = 0;
+  const int cnt = d.ij_count[i];
+  for (int k = 0; k < cnt; ++k) {
+    int j = d.ij_link[ELL(k, i)];
+    double temp = d.p[j] - pi_;
+    a = a + temp * d.wGx[ELL(k, i)];
+    b = b + temp * d.wGy[ELL(k, i)];
+  }
+  const double K11 = d.kgcm[0][i], K21 = d.kgcm[1][i], K12 = d.kgcm[2][i], K22 = d.kgcm[3][i];
+  double gx = K11 * a + K12 * b, gy = K21 * a + K22 * b;
+  d.gpx[i] = gx;
+  d.gpy[i] = gy;
+  const double dt = d.s->dt;
+  double ux = d.ux[i], uy = d.uy[i], x = d.rx[i], y = d.ry[i];
+  if (i >= c.nbS) {
+    ux = ux + dt * (c.bf[0] - gx);
+    uy = uy + dt * (c.bf[1] - gy);
+    if (cnt <= 3) {
+      ux = d.u0x[i] + dt * c.bf[0];
+      uy = d.u0y[i] + dt * c.bf[1];
+    }
+    x = d.r0x[i] + 0.5 * (ux + d.u0x[i]) * dt + d.ushx[i] * dt;
+    y = d.r0y[i] + 0.5 * (uy + d.u0y[i]) * dt + d.ushy[i] * dt;
+  }
+  d.ux2[i] = ux;
+  d.uy2[i] = uy;
+  d.rx2[i] = x;
+  d.ry2[i] = y;
+  atomic_max_pos(&d.s->absu_bits, fabs(ux));
+  atomic_max_pos(&d.s->absv_bits, fabs(uy));
+  atomic_max_pos(&d.s->absp_bits, fabs(pi_));
+}
+
+// secondary_properties: vorticity from final fluid u and mirror u* (div_free.F90:160-183)
+__global__ void k_secondary(Consts c, Dev d, const double* __restrict__ uxn, const double* __restrict__ uyn,
+                            const double* __restrict__ uxm, const double* __restrict__ uym) {
+  __shared__ double sh[TPB / 32 + 1];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double e = 0.0;
+  if (i < c.npfb) {
+    const double ui = uxn[i], vi = uyn[i];
+    double vt = 0.0;
+    const int cnt = d.ij_count[i];
+    for (int k = 0; k < cnt; ++k) {
+      int j = d.ij_link[ELL(k, i)];
+      double uj = j < c.npfb ? uxn[j] : uxm[j], vj = j < c.npfb ? uyn[j] : uym[j];
+      double tmp = (vi - vj) * d.wGx[ELL(k, i)] - (ui - uj) * d.wGy[ELL(k, i)];
+      vt = vt - tmp;
+    }
+    d.vort[i] = vt;
+    e = ui * ui + vi * vi;
+  }
+  double bs = block_sum<TPB>(e, sh);
+  if (threadIdx.x == 0) d.partials[blockIdx.x] = bs;
+}
+
+__global__ void k_secondary_final(Consts c, Dev d, int nblk) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s = 0.0;
+  for (int b = 0; b < nblk; ++b) s += d.partials[b];
+  d.s->rms_u = sqrt(s / (double)c.npfb);
+}
+
+void launch_weights_surface_shift(Ctx& x) {
+  const Consts& c = x.c;
+  int g = grid_for(c.npfb);
+  VEBI_LAUNCH(x, k_weights, g, TPB, c, x.d);
+  if (c.open_domain == 1) {
+    VEBI_LAUNCH(x, k_part_dist_vars, g, TPB, c, x.d);
+    VEBI_LAUNCH(x, k_nsurf_mirrors, x.gs_blocks, TPB, c, x.d);
+    VEBI_LAUNCH(x, k_smooth_normals, g, TPB, c, x.d);
+    VEBI_LAUNCH(x, k_copy_normals, g, TPB, c, x.d);
+  } else {
+    cudaMemsetAsync(x.d.n_surf, 0, sizeof(int) * (size_t)c.cap, x.st);
+  }
+  stage_mark(x, 5);
+  VEBI_LAUNCH(x, k_shift, g, TPB, c, x.d);
+}
+
+void launch_grad_mirrors(Ctx& x);
+void launch_mirror_stress(Ctx& x);
+void launch_mirror_velocities(Ctx& x);
+void launch_mirror_pressure(Ctx& x);
+
+void launch_predictor(Ctx& x) {
+  const Consts& c = x.c;
+  int g = grid_for(c.npfb);
+  stage_mark(x, 6);
+  VEBI_LAUNCH(x, k_gradients, g, TPB, c, x.d);
+  launch_grad_mirrors(x);
+  stage_mark(x, 7);
+  if (c.const_mod != 1) {
+    VEBI_LAUNCH(x, k_logconf, g, TPB, c, x.d);
+    launch_mirror_stress(x);
+  }
+  stage_mark(x, 8);
+  VEBI_LAUNCH(x, k_predictor, g, TPB, c, x.d);
+  launch_mirror_velocities(x);
+  // u*, theta* become the current buffers
+  std::swap(x.d.ux, x.d.ux2);
+  std::swap(x.d.uy, x.d.uy2);
+  std::swap(x.d.th, x.d.th2);
+}
+
+void launch_final(Ctx& x, int secondary) {
+  const Consts& c = x.c;
+  int g = grid_for(c.npfb);
+  stage_mark(x, 11);
+  launch_mirror_pressure(x);
+  VEBI_LAUNCH(x, k_pgrad_final, g, TPB, c, x.d);
+  // u^{n+1}, r^{n+1} become current; u*, r* stay in the second buffers
+  std::swap(x.d.ux, x.d.ux2);
+  std::swap(x.d.uy, x.d.uy2);
+  std::swap(x.d.rx, x.d.rx2);
+  std::swap(x.d.ry, x.d.ry2);
+  if (secondary) {
+    stage_mark(x, 13);
+    VEBI_LAUNCH(x, k_secondary, g, TPB, c, x.d, x.d.ux, x.d.uy, x.d.ux2, x.d.uy2);
+    VEBI_LAUNCH(x, k_secondary_final, 1, 32, c, x.d, g);
+  }
+}
+
+}  // namespace vebi

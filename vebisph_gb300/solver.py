@@ -1,0 +1,119 @@
+"""Host-side mirror of the reference's time step over the C-ABI (include/vebi.h).
+
+The Fortran driver calls `div_free(x_mint,y_mint,x_maxt,y_maxt)` once per step
+(source/base/sph2D_incom.F90:97) on state held in module globals; `StepSolver` holds the
+same state on the GPU and exposes the same call.  Every computation runs in the CUDA
+library; this module only moves host arrays and reads results.  It raises when the
+library is missing -- there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .cases import Case
+
+# intermediate arrays of the last step exposed by vebi_debug_get
+DEBUG_FIELDS = (
+    "rx", "ry", "ux", "uy", "theta", "p", "tau11", "tau21", "tau12", "tau22", "trace_conf", "a_out",
+    "vort", "n_surf", "irelation", "vrelation", "dP_mp", "rsx", "rsy", "cellpart", "ist", "cell_cnt",
+    "ij_count", "ij_link", "w_Gx", "w_Gy", "w_L", "kgcm11", "kgcm21", "kgcm12", "kgcm22", "gradu_x",
+    "gradu_y", "gradv_x", "gradv_y", "gradth_x", "gradth_y", "gradC_x", "gradC_y", "ushift_x",
+    "ushift_y", "ustar_x", "ustar_y", "theta_star", "ppe_B", "ppe_diag", "ppe_val", "ppe_col",
+    "grad_px", "grad_py", "conc", "div_r",
+)
+
+
+class VebiError(RuntimeError):
+    def __init__(self, status: int, where: str, detail: str = ""):
+        self.status = status
+        super().__init__(f"{where}: {abi.STATUS_NAMES.get(status, status)} {detail}".strip())
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class StepSolver:
+    """One GPU context holding one simulation's particle state."""
+
+    def __init__(self, case: Case, precision: int = abi.PREC_FP64, timing: bool = False):
+        self.lib = abi.load_library()
+        self.case = case
+        self.params = case.params(precision)
+        self.x_mint, self.x_maxt, self.y_mint, self.y_maxt = (
+            self.params.x_mint, self.params.x_maxt, self.params.y_mint, self.params.y_maxt)
+        h = C.c_void_p()
+        self._check(self.lib.vebi_create(C.byref(self.params), C.byref(h)), "vebi_create")
+        self.h = h
+        if timing:
+            self.lib.vebi_set_timing(self.h, 1)
+        f = case.fortran_planes()
+        self.upload(f["r"], f["u"], f["tau"], f["theta"], f["trace_conf"], f["inbin"], f["ld"])
+
+    def _check(self, st: int, where: str):
+        if st:
+            raise VebiError(st, where, self.lib.vebi_last_error().decode())
+
+    # -- state transfer ---------------------------------------------------------------
+    def upload(self, r, u, tau, theta, trace_conf, inbin, ld: int):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (r, u, tau, theta, trace_conf)]
+        ib = np.ascontiguousarray(inbin, dtype=np.uint8)
+        self._check(self.lib.vebi_upload_state(self.h, *[_dp(a) for a in arrs],
+                                               ib.ctypes.data_as(C.POINTER(C.c_uint8)), ld),
+                    "vebi_upload_state")
+
+    def download(self, ld: int | None = None) -> dict:
+        n = self.case.npfb
+        ld = ld or n
+        out = dict(r=np.zeros((2, ld)), u=np.zeros((2, ld)), tau=np.zeros((4, ld)), theta=np.zeros(ld),
+                   p=np.zeros(ld), vort=np.zeros(ld), a_out=np.zeros(ld), trace_conf=np.zeros(ld),
+                   n_surf=np.zeros(ld, np.int32), inbin=np.zeros(ld, np.uint8))
+        self._check(self.lib.vebi_download_state(
+            self.h, _dp(out["r"]), _dp(out["u"]), _dp(out["tau"]), _dp(out["theta"]), _dp(out["p"]),
+            _dp(out["vort"]), _dp(out["a_out"]), _dp(out["trace_conf"]),
+            out["n_surf"].ctypes.data_as(C.POINTER(C.c_int32)),
+            out["inbin"].ctypes.data_as(C.POINTER(C.c_uint8)), ld), "vebi_download_state")
+        return out
+
+    # -- the step ---------------------------------------------------------------------
+    def div_free(self, x_mint, y_mint, x_maxt, y_maxt, secondary: bool = False) -> dict:
+        """The reference's call signature (div_free.F90:22)."""
+        s = abi.VebiStepStats()
+        st = self.lib.vebi_step(self.h, x_mint, y_mint, x_maxt, y_maxt, int(secondary), C.byref(s))
+        d = s.as_dict()
+        d["status"] = st
+        self._check(st, "vebi_step")
+        return d
+
+    def step(self, secondary: bool = False) -> dict:
+        return self.div_free(self.x_mint, self.y_mint, self.x_maxt, self.y_maxt, secondary)
+
+    def run_steps(self, n: int) -> tuple[float, dict]:
+        ms = C.c_double(0.0)
+        s = abi.VebiStepStats()
+        self._check(self.lib.vebi_run_steps(self.h, self.x_mint, self.y_mint, self.x_maxt, self.y_maxt, n,
+                                            C.byref(ms), C.byref(s)), "vebi_run_steps")
+        return ms.value, s.as_dict()
+
+    # -- inspection -------------------------------------------------------------------
+    def get(self, name: str) -> np.ndarray:
+        esz, n = C.c_int64(), C.c_int64()
+        self._check(self.lib.vebi_debug_size(self.h, name.encode(), C.byref(esz), C.byref(n)), name)
+        out = np.empty(n.value, np.float64 if esz.value == 8 else np.int32)
+        self._check(self.lib.vebi_debug_get(self.h, name.encode(), out.ctypes.data_as(C.c_void_p), out.nbytes),
+                    name)
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.vebi_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
