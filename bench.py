@@ -1,0 +1,356 @@
+#!/usr/bin/env python3
+"""Benchmark of the vebisph time step on GB300: particle-steps/s of div_free.
+
+Default workload: the confined cylinder flow (channel 30R x 4R, blockage 0.5, ~4M fluid
+particles on a seeded jittered lattice, Oldroyd-B, Re=0.01, Wi=0.6, beta=0.59), FP64.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One JSON line on rank 0.  `value` is fluid particles x steps / device time of K steps with
+the state resident in HBM; `e2e` repeats the measurement through the C-ABI with the state
+copied host->device before and device->host after every step (pinned host arrays); the
+`roofline` object is for the dominant kernel (the persistent BiCGSTAB solver);
+`cpu_baseline` times the CPU restatement of the reference (the oracle; the Fortran reference
+cannot be compiled: no Fortran compiler on either machine) on this host's cores.
+For N > 1 (torchrun) every rank runs an independent replica on its own GPU (the step does
+not shard); `value` sums the ranks' particle-steps over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-steps/s @4M (mixed vs FP64 GPU, 1e-4 rel err); adjoint/forward cost"
+UNIT = "particle-steps/s"
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Dist:
+    """Replica bookkeeping: torch.distributed (gloo) only for barriers and the max of times."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_rank{gpu_index}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self) -> dict:
+        if not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        rows = [ln.split(",") for ln in self.path.read_text().splitlines() if ln.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]), "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows)}
+
+
+def make_case(args):
+    from vebisph_gb300 import cases
+    if args.case == "cylinder_4m":
+        return cases.cylinder(args.particles, Wi=args.wi, seed=args.seed)
+    if args.case == "poiseuille_1m":
+        return cases.poiseuille(1000, seed=args.seed)
+    if args.case == "cavity_1m":
+        return cases.cavity(1024, seed=args.seed)
+    raise SystemExit(f"unknown case {args.case}")
+
+
+def ppe_bytes_per_iteration(n_rows: int, nnz_off: int) -> float:
+    """Algorithmic bytes of one fused BiCGSTAB iteration (closed domain, FP64):
+    2 SpMV x (12 B per off-diagonal slot + 44 B per row: count, diagonal, x_i, gathered x,
+    y, one dot operand) + 168 B per row of vector phases (p update 32, mean removal 24, s 24,
+    s mean removal 24, x/r update 64)."""
+    return 2.0 * (12.0 * nnz_off + 44.0 * n_rows) + 168.0 * n_rows
+
+
+def cpu_baseline(case, gpu_iters_per_step: float, itermax_sample: int):
+    """Time the oracle (CPU restatement of the reference) on this host's cores on a bounded
+    sample: one full step whose BiCGSTAB is capped at itermax_sample iterations; the step time
+    is scaled to the GPU's iterations per step: t = t_rest + t_solve/iters_sample*iters_gpu."""
+    from oracle.oracle import OracleSolver, threads
+    o = OracleSolver(case)
+    o.set_itermax(itermax_sample)
+    o.step()  # warm-up (first touch of the arrays)
+    t0 = time.perf_counter()
+    s = o.step()
+    wall = (time.perf_counter() - t0) * 1e3
+    total, solve, iters = s["stage_ms"][14], s["stage_ms"][10], max(s["LS_iters"], 1)
+    rest = total - solve
+    per_iter = solve / iters
+    t_step = rest + per_iter * gpu_iters_per_step
+    o.close()
+    value = case.n_fluid / (t_step * 1e-3)
+    return {"value": value, "unit": UNIT, "cores": threads(), "kind": "port",
+            "sample": (f"one oracle step of the same case with BiCGSTAB capped at {itermax_sample} "
+                       f"iterations ({iters} run): non-solver {rest:.0f} ms + {per_iter:.1f} ms/iteration "
+                       f"scaled to {gpu_iters_per_step:.0f} iterations/step = {t_step:.0f} ms/step; "
+                       f"wall {wall:.0f} ms")}
+
+
+def run_gb300(args, dist: Dist):
+    from vebisph_gb300 import abi
+    from vebisph_gb300.solver import StepSolver
+    import ctypes as C
+
+    case = make_case(args)
+    if args.itermax:
+        case.itermax = args.itermax
+    prec = abi.PREC_MIXED if args.precision == "mixed" else abi.PREC_FP64
+    sol = StepSolver(case, precision=prec, timing=True)
+    n_fluid = case.n_fluid
+    # warm-up steps (untimed)
+    for _ in range(args.warmup):
+        sol.step()
+    dist.barrier()
+    with ClockSampler(dist.local) as clk:
+        ms, st = sol.run_steps(args.steps)
+    dist.barrier()
+    t_max = dist.max(ms)
+    units = dist.sum(float(n_fluid * args.steps))
+    value = units / (t_max * 1e-3)
+    ls_total = st["LS_iters_total"]
+    iters_per_step = ls_total / args.steps
+    stage = st["stage_ms"]
+    solve_ms = stage[10]
+    # roofline of the dominant kernel: the persistent BiCGSTAB launch (one per step)
+    cnt = sol.get("ij_count")
+    nnz_off = int(cnt.sum())
+    bytes_iter = ppe_bytes_per_iteration(case.npfb, nnz_off)
+    per_launch_bytes = bytes_iter * iters_per_step
+    per_launch_s = solve_ms * 1e-3 / args.steps
+    achieved = per_launch_bytes / per_launch_s / 1e9
+    peak, peak_kind = peaks()
+    traffic = None
+    tf = ROOT / "profiles" / "traffic_bicgstab.json"
+    if tf.exists():
+        tj = json.loads(tf.read_text())
+        # measured DRAM bytes per iteration on a small case, scaled by rows x iterations
+        traffic = tj["dram_bytes_per_row_iteration"] * case.npfb * iters_per_step
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic,
+            "kernel": "k_bicgstab<true> (persistent cooperative BiCGSTAB, one launch per step)",
+            "peak_kind": f"{peak_kind} hbm_gbs (burst copy)",
+            "bytes_per_iteration": bytes_iter, "iterations_per_launch": iters_per_step,
+            "launch_ms": round(per_launch_s * 1e3, 3)}
+    # end to end through the C-ABI with host buffers (pinned), copies inside the timed region
+    e2e = None
+    if not args.no_e2e:
+        f = case.fortran_planes()
+        host = {k: np.ascontiguousarray(v) for k, v in f.items() if k != "ld"}
+        out = {k: np.zeros_like(host[k]) for k in ("r", "u", "tau", "theta")}
+        out["p"] = np.zeros(case.npfb)
+        pinned = []
+        for a in list(host.values()) + list(out.values()):
+            if sol.lib.vebi_pin_host(a.ctypes.data_as(C.c_void_p), a.nbytes) == 0:
+                pinned.append(a)
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+        # start from the state the GPU holds now (as a driver that owns the host arrays would)
+        sol.download()
+        h2d = sum(host[k].nbytes for k in ("r", "u", "tau", "theta", "trace_conf", "inbin"))
+        d2h = sum(out[k].nbytes for k in ("r", "u", "tau", "theta", "p"))
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            sol.upload(host["r"], host["u"], host["tau"], host["theta"], host["trace_conf"], host["inbin"],
+                       f["ld"])
+            sol.step()
+            sol.lib.vebi_download_state(sol.h, dp(out["r"]), dp(out["u"]), dp(out["tau"]), dp(out["theta"]),
+                                        dp(out["p"]), None, None, None, None, None, f["ld"])
+        e2e_s = time.perf_counter() - t0
+        dist.barrier()
+        e2e_s = dist.max(e2e_s)
+        for a in pinned:
+            sol.lib.vebi_unpin_host(a.ctypes.data_as(C.c_void_p))
+        e2e = {"value": dist.sum(float(n_fluid * args.e2e_steps)) / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
+               "path": "vebi_upload_state + vebi_step + vebi_download_state (pinned host arrays)"}
+    res = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == abi.PREC_FP64 else "f32+f64",
+        "data": "synthetic: seeded jittered lattice (U(-0.01dx,0.01dx)), walls/circle by the reference's "
+                "make_boundary_particles rules; no dataset",
+        "config": {"workload": f"{case.name}: confined cylinder, channel 30R x 4R, blockage 0.5, "
+                               f"{n_fluid} fluid + {case.nbS} wall particles, dx={case.dx:.4g}, Oldroyd-B "
+                               f"Re=0.01 Wi={args.wi} beta=0.59, periodic x, {args.precision}",
+                   "npfb": case.npfb, "n_fluid": n_fluid, "precision": args.precision,
+                   "parallelism": f"replicas x{dist.world}",
+                   "l2": "inputs larger than L2 (ELL matrix and pair arrays are several GB)"},
+        "LS_iters_per_step": iters_per_step,
+        "LS_residual_last": st["LS_residual"],
+        "stage_ms_per_step": {abi.STAGE_NAMES[i]: round(v / args.steps, 3) for i, v in enumerate(stage) if v > 0},
+        "gpu_launches": st["gpu_launches"],
+        "roofline": roof,
+        "e2e": e2e,
+        "clocks": clk.summary(),
+        "nmirror": st["nmirror"], "maxneighbours": st["maxneighbours"],
+    }
+    sol.close()
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu:
+        res["cpu_baseline"] = cpu_baseline(case, iters_per_step, args.cpu_iters)
+    return res
+
+
+def run_reference(args, dist: Dist):
+    """The reference's own CPU path timed on this host: the oracle restatement (the Fortran
+    reference has no compiler here), all host threads, each step a bounded sample."""
+    if dist.rank != 0:
+        return None
+    from oracle.oracle import OracleSolver, threads
+    case = make_case(args)
+    o = OracleSolver(case)
+    o.set_itermax(args.cpu_iters)
+    for _ in range(args.warmup):
+        o.step()
+    tot = 0.0
+    solve = 0.0
+    iters = 0
+    for _ in range(args.steps):
+        s = o.step()
+        tot += s["stage_ms"][14]
+        solve += s["stage_ms"][10]
+        iters += s["LS_iters"]
+    per_iter = solve / max(iters, 1)
+    rest = (tot - solve) / args.steps
+    t_step = rest + per_iter * args.ref_iters
+    value = case.n_fluid / (t_step * 1e-3)
+    sample = (f"{args.steps} oracle steps, BiCGSTAB capped at {args.cpu_iters} iterations; "
+              f"non-solver {rest:.0f} ms/step + {per_iter:.1f} ms/iteration scaled to {args.ref_iters} "
+              f"iterations/step")
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (same generator and seed as the GPU arm)",
+            "config": {"workload": f"{case.name}: confined cylinder, {case.n_fluid} fluid particles",
+                       "npfb": case.npfb, "n_fluid": case.n_fluid, "precision": "fp64"},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads(), "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--case", default="cylinder_4m")
+    ap.add_argument("--particles", type=float, default=4.0e6)
+    ap.add_argument("--wi", type=float, default=0.6)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-iters", type=int, default=20, help="BiCGSTAB cap of the CPU sample")
+    ap.add_argument("--ref-iters", type=float, default=1001.0,
+                    help="iterations/step the reference-arm sample is scaled to")
+    ap.add_argument("--itermax", type=int, default=0, help="override the PPE iteration cap (profiling runs)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    dist = Dist()
+    if args.impl == "gb300":
+        import __graft_entry__ as g
+        if dist.local == 0 or not (ROOT / "vebisph_gb300" / "_build" / "libvebi_gb300.so").exists():
+            g.build()
+        dist.barrier()
+        if dist.world > 1:
+            # one replica per GPU: pin this rank to its local GPU before the first CUDA call
+            vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+            ids = vis.split(",") if vis else [str(i) for i in range(dist.world)]
+            os.environ["CUDA_VISIBLE_DEVICES"] = ids[dist.local % len(ids)]
+        res = run_gb300(args, dist)
+    else:
+        from oracle import build as ob
+        ob.build()
+        res = run_reference(args, dist)
+    if dist.rank == 0 and res is not None:
+        print(json.dumps(res))
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -120,9 +120,10 @@ typedef struct vebi_step_stats {
   int32_t n_escapees;
   int32_t error;        /* first device-side error code of the step (0 = none)       */
   int32_t warnings;     /* VEBI_WARN_* bits                                          */
-  int32_t gpu_launches; /* kernels this library launched during the step             */
+  int32_t gpu_launches; /* kernels this library launched during the step(s)          */
   int32_t refine_iters; /* mixed precision: outer refinement sweeps                  */
-  int32_t pad;
+  int32_t LS_iters_total; /* vebi_run_steps: BiCGSTAB iterations summed over the steps */
+  int32_t nsteps;       /* steps these statistics cover                              */
 } vebi_step_stats;
 
 typedef struct vebi_ctx vebi_ctx;
@@ -146,7 +147,8 @@ int vebi_step(vebi_ctx* ctx, double x_mint, double y_mint, double x_maxt, double
               int32_t secondary, vebi_step_stats* stats);
 
 /* Run nsteps steps back to back on the context's stream (no host copies) and return
- * the device time between the first launch and the last completion in *ms. */
+ * the device time between the first launch and the last completion in *ms.  With timing
+ * on, last->stage_ms holds each stage's device time summed over the nsteps steps. */
 int vebi_run_steps(vebi_ctx* ctx, double x_mint, double y_mint, double x_maxt, double y_maxt,
                    int32_t nsteps, double* ms, vebi_step_stats* last);
 

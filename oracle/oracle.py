@@ -29,6 +29,7 @@ def load():
         lib.orc_step.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
                                  P(abi.VebiStepStats)]
         lib.orc_box.argtypes = [vp, P(C.c_double), P(C.c_int)]
+        lib.orc_set_itermax.argtypes = [vp, C.c_int]
         lib.orc_size.argtypes = [vp, C.c_char_p, P(C.c_int64), P(C.c_int64)]
         lib.orc_get.argtypes = [vp, C.c_char_p, vp, C.c_int64]
         lib.orc_kernel_w.argtypes = [vp, C.c_double]
@@ -90,6 +91,9 @@ class OracleSolver:
         out = np.empty(n.value, dt)
         self.lib.orc_get(self.h, name.encode(), out.ctypes.data_as(C.c_void_p), out.nbytes)
         return out
+
+    def set_itermax(self, itermax: int):
+        self.lib.orc_set_itermax(self.h, int(itermax))
 
     def W(self, q: float) -> float:
         return self.lib.orc_kernel_w(self.h, q)

@@ -95,6 +95,14 @@ struct Oracle {
   int n_inbin = 0, n_escapees = 0, error = 0, warnings = 0;
   double ppe_rhs_mean = 0, rms_u = 0;
   int maxneighbours = 0;
+  double t_solve_ms = 0.0, t_step_ms = 0.0;  // per-step wall times (CPU baseline)
+  static double wtime() {
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    return 0.0;
+#endif
+  }
 
   // particle fields, capacity cap = npfb + mirror capacity
   std::vector<double> rx, ry, ux, uy, theta, p, tau[4], trace_conf, a_out, vort, conc, div_r;
@@ -1283,7 +1291,11 @@ struct Oracle {
       }
     }
     std::vector<double> x(npfb, 0.0);
+    mark(10);
+    double t0 = wtime();
     bicgstab(x, ppe_B, P.i_open_domain == 0);
+    t_solve_ms = (wtime() - t0) * 1e3;
+    mark(9);
     for (int i = 0; i < npfb; ++i) p[i] = x[i];
   }
 
@@ -1324,6 +1336,29 @@ struct Oracle {
 
   // ------------------------------------------------------------------ div_free
   int step(double xmn, double ymn, double xmx, double ymx, int secondary) {
+    double t0 = wtime();
+    int st = step_body(xmn, ymn, xmx, ymx, secondary);
+    t_step_ms = (wtime() - t0) * 1e3;
+    return st;
+  }
+  double stage_t[VEBI_NSTAGES] = {};
+  double tmark = 0.0;
+  int tstage = -1;
+  void mark(int s) {  // per-stage wall time, same stage numbering as the GPU library
+    double t = wtime();
+    if (tstage >= 0 && tstage < VEBI_NSTAGES) stage_t[tstage] += (t - tmark) * 1e3;
+    tstage = s;
+    tmark = t;
+  }
+  int step_body(double xmn, double ymn, double xmx, double ymx, int secondary) {
+    for (auto& v : stage_t) v = 0.0;
+    tstage = -1;
+    mark(0);
+    int st = step_stages(xmn, ymn, xmx, ymx, secondary);
+    mark(-1);
+    return st;
+  }
+  int step_stages(double xmn, double ymn, double xmx, double ymx, int secondary) {
     error = 0; warnings = 0; n_escapees = 0;
     // STEP 1 (div_free.F90:39-41)
     r0x.assign(2 * npfb, 0.0); r0y.assign(2 * npfb, 0.0);
@@ -1336,29 +1371,37 @@ struct Oracle {
     // STEP 4
     int st = put_in_bin(xmn, xmx, ymn, ymx);
     if (st) return st;
+    mark(1);
     st = create_mirror_particles();
     if (st) return st;
     if (n_escapees) warnings |= VEBI_WARN_ESCAPEES;
     rsx.assign(rx.begin(), rx.begin() + np); rsy.assign(ry.begin(), ry.begin() + np);
+    mark(2);
     st = divide();
     if (st) return st;
+    mark(3);
     st = neighbour_list();
     if (st) return st;
+    mark(4);
     kernel_calculation();
     locate_free_surf_part();
+    mark(5);
     // STEP 5
     ushx.assign(npfb, 0.0); ushy.assign(npfb, 0.0);
     new_fick_shift();
     for (int i = 0; i < npfb; ++i) { ushx[i] = drx[i] / dt; ushy[i] = dry[i] / dt; }
     for (int i = 0; i < nbS; ++i) { ushx[i] = -ux[i]; ushy[i] = -uy[i]; }
     // STEP 7
+    mark(8);
     prediction_step();
     // STEP 8
     mirror_velocities();
+    mark(9);
     ustx.assign(ux.begin(), ux.begin() + np); usty.assign(uy.begin(), uy.begin() + np);
     thst.assign(theta.begin(), theta.begin() + npfb);
     ppe_solve();
     // STEP 9
+    mark(11);
     calc_pressure_gradient();
     for (int i = nbS; i < npfb; ++i) {
       ux[i] = ux[i] + dt * (P.body_force[0] - gpx[i]);
@@ -1369,7 +1412,9 @@ struct Oracle {
       }
     }
     // STEP 11
+    mark(13);
     if (secondary) secondary_properties();
+    mark(12);
     // STEP 12
     for (int i = nbS; i < npfb; ++i) {
       rx[i] = r0x[i] + 0.5 * (ux[i] + u0x[i]) * dt + ushx[i] * dt;
@@ -1392,6 +1437,10 @@ struct Oracle {
     s->LS_iters = LS_iters; s->n_inbin = n_inbin; s->np = np; s->npfb = npfb;
     s->nmirror = nmirror; s->maxneighbours = maxneighbours; s->n_escapees = n_escapees;
     s->error = error; s->warnings = warnings;
+    for (int q = 0; q < VEBI_NSTAGES; ++q) s->stage_ms[q] = stage_t[q];
+    s->stage_ms[10] = t_solve_ms;   // PPE solve
+    s->stage_ms[14] = t_step_ms;    // whole step
+    s->LS_iters_total = LS_iters; s->nsteps = 1;
   }
 
   // ------------------------------------------------------------------ inspection
@@ -1480,6 +1529,10 @@ int orc_step(void* h, double xmn, double ymn, double xmx, double ymx, int second
   int s = o->step(xmn, ymn, xmx, ymx, secondary);
   if (st) { o->fill_stats(st); st->error = s; }
   return s;
+}
+int orc_set_itermax(void* h, int itermax) {
+  static_cast<Oracle*>(h)->P.itermax = itermax;
+  return 0;
 }
 int orc_box(void* h, double* box4, int* ncxy) {
   auto* o = static_cast<Oracle*>(h);

@@ -70,7 +70,8 @@ class VebiStepStats(C.Structure):
         ("LS_iters", C.c_int32), ("n_inbin", C.c_int32),
         ("np", C.c_int32), ("npfb", C.c_int32), ("nmirror", C.c_int32), ("maxneighbours", C.c_int32),
         ("n_escapees", C.c_int32), ("error", C.c_int32), ("warnings", C.c_int32),
-        ("gpu_launches", C.c_int32), ("refine_iters", C.c_int32), ("pad", C.c_int32),
+        ("gpu_launches", C.c_int32), ("refine_iters", C.c_int32),
+        ("LS_iters_total", C.c_int32), ("nsteps", C.c_int32),
     ]
 
     def as_dict(self) -> dict:

@@ -324,6 +324,8 @@ static int finish_step(Ctx& x, vebi_step_stats* stats, bool sync) {
   o.warnings = s.warnings | (s.n_escapees ? VEBI_WARN_ESCAPEES : 0);
   o.gpu_launches = x.launches;
   o.refine_iters = s.refine_iters;
+  o.LS_iters_total = s.ls_iters_total;
+  o.nsteps = 1;
   if (x.timing && sync) {
     int prev = -1;
     for (int q = 0; q <= VEBI_NSTAGES; ++q) {
@@ -381,19 +383,57 @@ int vebi_run_steps(vebi_ctx* h, double x_mint, double y_mint, double x_maxt, dou
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  bool timing = x.timing;
-  x.timing = false;
+  const int NE = VEBI_NSTAGES + 1;
+  std::vector<cudaEvent_t> evs;
+  std::vector<std::vector<bool>> used;
+  if (x.timing) {
+    evs.resize((size_t)nsteps * NE);
+    for (auto& e : evs) cudaEventCreate(&e);
+    x.ev_run = evs.data();
+  }
   x.launches = 0;
+  cudaMemsetAsync(&x.d.s->ls_iters_total, 0, sizeof(int), x.st);
   cudaEventRecord(e0, x.st);
-  for (int s = 0; s < nsteps; ++s) enqueue_step(x, 0);
+  for (int s = 0; s < nsteps; ++s) {
+    if (x.timing) x.ev_run_step = s;
+    enqueue_step(x, 0);
+    if (x.timing) {
+      cudaEventRecord(evs[(size_t)s * NE + VEBI_NSTAGES], x.st);
+      used.emplace_back(x.ev_used, x.ev_used + VEBI_NSTAGES);
+    }
+  }
+  x.ev_run_step = -1;
   cudaEventRecord(e1, x.st);
+  bool timing = x.timing;
+  x.timing = false;  // finish_step must not read the single-step events
   int st = finish_step(x, last, true);
+  x.timing = timing;
   float t = 0.f;
   cudaEventElapsedTime(&t, e0, e1);
   if (ms) *ms = t;
+  if (last) {
+    last->nsteps = nsteps;
+    if (x.timing) {
+      for (int q = 0; q < VEBI_NSTAGES; ++q) last->stage_ms[q] = 0.0;
+      for (int s = 0; s < nsteps; ++s) {
+        int prev = -1;
+        for (int q = 0; q <= VEBI_NSTAGES; ++q) {
+          bool u = q == VEBI_NSTAGES || used[s][q];
+          if (!u) continue;
+          if (prev >= 0) {
+            float m = 0.f;
+            cudaEventElapsedTime(&m, evs[(size_t)s * NE + prev], evs[(size_t)s * NE + q]);
+            last->stage_ms[prev] += m;
+          }
+          prev = q;
+        }
+      }
+    }
+  }
+  for (auto& e : evs) cudaEventDestroy(e);
+  x.ev_run = nullptr;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  x.timing = timing;
   return st;
 }
 

@@ -65,6 +65,7 @@ struct Scal {
   int bar_count;                     // grid barrier state of the PPE kernel
   unsigned int bar_gen;
   int refine_iters;
+  int ls_iters_total;                // summed over the steps of one vebi_run_steps call
 };
 
 // Device arrays of one context.  Particle fields have capacity cap = npfb + mcap and are

@@ -20,6 +20,8 @@ struct Ctx {
   bool timing = false;
   cudaEvent_t ev[VEBI_NSTAGES + 1]{};
   bool ev_used[VEBI_NSTAGES]{};
+  cudaEvent_t* ev_run = nullptr;   // per-step stage events of vebi_run_steps (timing on)
+  int ev_run_step = -1;            // step whose events stage_mark records, -1 = use ev[]
   int coop_blocks = 0;       // persistent PPE grid (co-resident blocks)
   int gs_blocks = 0;         // grid of grid-stride kernels over dynamic counts
   int sel_max_blocks = 0;    // blocks of the ordered-select kernels
@@ -45,7 +47,8 @@ inline int grid_for(long long n, int tpb = TPB) {
 // stage timers: record the start event of stage `s` (ends at the next recorded stage)
 inline void stage_mark(Ctx& x, int s) {
   if (!x.timing) return;
-  cudaEventRecord(x.ev[s], x.st);
+  if (x.ev_run_step >= 0) cudaEventRecord(x.ev_run[(size_t)x.ev_run_step * (VEBI_NSTAGES + 1) + s], x.st);
+  else cudaEventRecord(x.ev[s], x.st);
   x.ev_used[s] = true;
 }
 

@@ -337,6 +337,7 @@ __global__ void __launch_bounds__(TPB) k_bicgstab(Consts c, Dev d) {
   for (int i = tid; i < n; i += stride) d.p[i] = x[i];
   if (tid == 0) {
     s->ls_iters = iter;
+    s->ls_iters_total += iter;
     s->ls_residual = resid;
     atomicOr(&s->warnings, warn);
   }
