@@ -64,18 +64,35 @@ def test_neighbour_sets_order_normalised(libs):
 
 
 def test_multistep_poiseuille_fields(libs):
-    """20 steps: the fields stay within 1e-6 of the oracle (reduction order only)."""
+    """20 steps: u and r stay within 1e-6 of the oracle; tau within the oracle's own spread.
+
+    GPU and oracle differ only by the order of the PPE reductions (~1e-13 relative in u per
+    step).  The log-conformation update divides by (lambda2 - lambda1 + 1e-10)
+    (predictor_mod.F90:213), which is near 1e-10 while the conformation tensor is close to the
+    identity, so such differences are amplified in tau.  The test measures that amplification
+    on the oracle itself -- a second oracle run whose velocity is perturbed by 1e-13 after the
+    first step -- and requires the GPU to be no further from the oracle than 10x that spread."""
     StepSolver, OracleSolver = libs
     case = cases.poiseuille(40, seed=7)
-    gpu, ref = StepSolver(case), OracleSolver(case)
-    for _ in range(20):
-        sg, so = gpu.step(), ref.step()
+    gpu, ref, pert = StepSolver(case), OracleSolver(case), OracleSolver(case)
     n = case.npfb
-    # errors relative to the size of the vector / tensor field they belong to
-    groups = {"u": ("ux", "uy"), "r": ("rx", "ry"), "tau": ("tau11", "tau12", "tau21", "tau22")}
+    for k in range(20):
+        sg, so = gpu.step(), ref.step()
+        pert.step()
+        if k == 0:
+            r = np.stack([pert.get("rx")[:n], pert.get("ry")[:n]])
+            u = np.stack([pert.get("ux")[:n], pert.get("uy")[:n]]) * (1.0 + 1e-13)
+            tau = np.stack([pert.get(nm)[:n] for nm in ("tau11", "tau21", "tau12", "tau22")])
+            pert.upload(r, u, tau, pert.get("theta")[:n], pert.get("trace_conf"), np.zeros(n, np.uint8), n)
+    groups = {"u": ("ux", "uy"), "r": ("rx", "ry")}
     for names in groups.values():
         scale = max(max(np.abs(ref.get(nm)[:n]).max() for nm in names), 1e-30)
         for name in names:
             a, b = gpu.get(name)[:n], ref.get(name)[:n]
             assert np.abs(a - b).max() / scale < 1e-6, name
+    for name in ("tau11", "tau12", "tau21", "tau22"):
+        a, b, c = gpu.get(name)[:n], ref.get(name)[:n], pert.get(name)[:n]
+        spread = np.abs(c - b).max()
+        scale = np.abs(b).max()
+        assert np.abs(a - b).max() <= 10.0 * spread + 1e-12 * scale, name
     assert abs(sg["dt"] - so["dt"]) <= 1e-9 * so["dt"]
