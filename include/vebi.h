@@ -176,6 +176,26 @@ int vebi_set_timing(vebi_ctx* ctx, int32_t on);
 int vebi_debug_size(vebi_ctx* ctx, const char* name, int64_t* elem_bytes, int64_t* count);
 int vebi_debug_get(vebi_ctx* ctx, const char* name, void* out, int64_t bytes);
 
+/* ---- A PPE solve that allocates nothing.  No counterpart in the reference. ------------
+ * For callers that cannot call cudaMalloc -- a host framework whose allocator owns all device
+ * memory, or a real-time loop that must not allocate -- this runs the step's BiCGSTAB
+ * (SPARSE_PBICGSTAB_nonull when closed_domain != 0, else the Jacobi SPARSE_PBICGSTAB) on a
+ * matrix the caller already holds in device memory, in the layout of vebi_debug_get's
+ * ij_count / ppe_col / ppe_val / ppe_diag / ppe_B (ELL [k][i] with stride ell_stride >= n),
+ * with x0 = 0, and writes x.  Its working vectors live in a file-scope device array of fixed
+ * size (about 4.3 MB, held by every GPU that loads the library until the process exits), so:
+ *  - n is at most VEBI_NOALLOC_MAX_ROWS; larger n returns VEBI_ERR_ARG;
+ *  - all calls share that array: calls that overlap on the GPU race;
+ *  - the first call on a device looks up the array's device address with that device
+ *    current; make that first call before any stream capture begins.
+ * `stream` is a cudaStream_t (NULL = legacy default stream).  When iters_out or residual_out
+ * is non-NULL the call waits for the solve and reports them. */
+#define VEBI_NOALLOC_MAX_ROWS 65536
+int vebi_ppe_solve_noalloc(const int32_t* ij_count, const int32_t* ppe_col, const double* ppe_val,
+                           const double* ppe_diag, const double* rhs, double* x, int32_t n,
+                           int64_t ell_stride, int32_t closed_domain, double tol, int32_t itermax,
+                           void* stream, int32_t* iters_out, double* residual_out);
+
 /* Static description of the library build. */
 const char* vebi_version(void);
 

@@ -96,8 +96,9 @@ LIB_NAME = "libvebi_gb300.so"
 EXPORTED_SYMBOLS = [
     "vebi_create", "vebi_upload_state", "vebi_step", "vebi_run_steps", "vebi_download_state",
     "vebi_destroy", "vebi_pin_host", "vebi_unpin_host", "vebi_set_timing", "vebi_debug_size",
-    "vebi_debug_get", "vebi_version", "vebi_last_error",
+    "vebi_debug_get", "vebi_version", "vebi_last_error", "vebi_ppe_solve_noalloc",
 ]
+NOALLOC_MAX_ROWS = 65536
 
 _lib = None
 
@@ -134,6 +135,9 @@ def load_library():
     lib.vebi_set_timing.argtypes = [vp, C.c_int32]
     lib.vebi_debug_size.argtypes = [vp, C.c_char_p, P(C.c_int64), P(C.c_int64)]
     lib.vebi_debug_get.argtypes = [vp, C.c_char_p, vp, C.c_int64]
+    lib.vebi_ppe_solve_noalloc.argtypes = [vp, vp, vp, vp, vp, vp, C.c_int32, C.c_int64, C.c_int32,
+                                           C.c_double, C.c_int32, vp, P(C.c_int32), P(C.c_double)]
+    lib.vebi_ppe_solve_noalloc.restype = C.c_int
     lib.vebi_version.restype = C.c_char_p
     lib.vebi_last_error.restype = C.c_char_p
     for fn in ("vebi_create", "vebi_upload_state", "vebi_step", "vebi_run_steps", "vebi_download_state",

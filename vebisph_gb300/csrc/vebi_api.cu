@@ -240,6 +240,9 @@ const char* vebi_version(void) {
 
 const char* vebi_last_error(void) { return g_err.c_str(); }
 
+// error text of entry points defined in other translation units
+void vebi_set_last_error_internal(const char* msg) { g_err = msg ? msg : ""; }
+
 int vebi_create(const vebi_params* params, vebi_ctx** out) {
   if (!params || !out) return fail(VEBI_ERR_ARG, "null argument");
   *out = nullptr;
