@@ -215,7 +215,7 @@ static int allocate_all(Ctx& x) {
   }
   A_(d.ppe_B, n); A_(d.ppe_diag, n); A_(d.ppe_val, E); A_(d.ppe_col, E);
   A_(d.bx, n); A_(d.br, n); A_(d.brb, n); A_(d.bv, n); A_(d.bp, n); A_(d.bpi, n);
-  A_(d.bs, n); A_(d.bsi, n); A_(d.bt, n);
+  A_(d.bs, n); A_(d.bsi, n); A_(d.bt, n); A_(d.bM, n);
   size_t np_part = (size_t)grid_for(c.npfb);
   size_t coop_part = (size_t)x.coop_blocks * 12;
   A_(d.partials, (np_part > coop_part ? np_part : coop_part) + 64);
@@ -302,7 +302,6 @@ int vebi_upload_state(vebi_ctx* h, const double* r, const double* u, const doubl
 static int finish_step(Ctx& x, vebi_step_stats* stats, bool sync) {
   Scal s;
   CUDA_TRY(cudaMemcpyAsync(&s, x.d.s, sizeof(Scal), cudaMemcpyDeviceToHost, x.st));
-  if (x.timing) cudaEventRecord(x.ev[VEBI_NSTAGES], x.st);
   if (sync) CUDA_TRY(cudaStreamSynchronize(x.st));
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(VEBI_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
@@ -364,6 +363,54 @@ static void enqueue_step(Ctx& x, int secondary) {
   launch_final(x, secondary);
 }
 
+// Capture one step (without the dump-time diagnostic) into a CUDA graph, once per context and
+// timing mode; later steps replay it with one launch.  Every kernel argument of a step is the
+// same from step to step (counts live in device memory), so one capture serves all steps.
+// If capture is not possible the step is launched kernel by kernel instead.
+static bool graph_ready(Ctx& x) {
+  const int m = x.timing ? 1 : 0;
+  if (x.graph[m]) return true;
+  if (x.graph_failed[m]) return false;
+  cudaGraph_t g = nullptr;
+  x.launches = 0;
+  for (int q = 0; q < VEBI_NSTAGES; ++q) x.ev_used[q] = false;
+  if (cudaStreamBeginCapture(x.st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    x.graph_failed[m] = true;
+    return false;
+  }
+  x.capturing = true;
+  enqueue_step(x, 0);
+  if (x.timing) cudaEventRecordWithFlags(x.ev[VEBI_NSTAGES], x.st, cudaEventRecordExternal);
+  x.capturing = false;
+  cudaError_t e = cudaStreamEndCapture(x.st, &g);
+  cudaGraphExec_t ge = nullptr;
+  if (e == cudaSuccess && g) e = cudaGraphInstantiate(&ge, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (e != cudaSuccess || !ge) {
+    cudaGetLastError();
+    x.graph_failed[m] = true;
+    return false;
+  }
+  x.graph[m] = ge;
+  x.graph_launches[m] = x.launches;
+  for (int q = 0; q < VEBI_NSTAGES; ++q) x.graph_used[m][q] = x.ev_used[q];
+  return true;
+}
+
+// enqueue one step: the captured graph when possible, else kernel by kernel
+static void launch_step(Ctx& x, int secondary) {
+  if (!secondary && graph_ready(x)) {
+    const int m = x.timing ? 1 : 0;
+    cudaGraphLaunch(x.graph[m], x.st);
+    x.launches += x.graph_launches[m];
+    for (int q = 0; q < VEBI_NSTAGES; ++q) x.ev_used[q] = x.graph_used[m][q];
+    return;
+  }
+  enqueue_step(x, secondary);
+  if (x.timing && !x.capturing) cudaEventRecord(x.ev[VEBI_NSTAGES], x.st);
+}
+
 int vebi_step(vebi_ctx* h, double x_mint, double y_mint, double x_maxt, double y_maxt, int32_t secondary,
               vebi_step_stats* stats) {
   if (!h) return fail(VEBI_ERR_ARG, "null context");
@@ -372,7 +419,7 @@ int vebi_step(vebi_ctx* h, double x_mint, double y_mint, double x_maxt, double y
   if (x_mint != x.c.x_mint || x_maxt != x.c.x_maxt || y_mint != x.c.y_mint || y_maxt != x.c.y_maxt)
     return fail(VEBI_ERR_ARG, "domain box differs from the one the context was created with");
   x.launches = 0;
-  enqueue_step(x, secondary);
+  launch_step(x, secondary);
   return finish_step(x, stats, true);
 }
 
@@ -386,29 +433,31 @@ int vebi_run_steps(vebi_ctx* h, double x_mint, double y_mint, double x_maxt, dou
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  const int NE = VEBI_NSTAGES + 1;
-  std::vector<cudaEvent_t> evs;
-  std::vector<std::vector<bool>> used;
-  if (x.timing) {
-    evs.resize((size_t)nsteps * NE);
-    for (auto& e : evs) cudaEventCreate(&e);
-    x.ev_run = evs.data();
-  }
+  double acc[VEBI_NSTAGES] = {};
   x.launches = 0;
   cudaMemsetAsync(&x.d.s->ls_iters_total, 0, sizeof(int), x.st);
   cudaEventRecord(e0, x.st);
   for (int s = 0; s < nsteps; ++s) {
-    if (x.timing) x.ev_run_step = s;
-    enqueue_step(x, 0);
+    launch_step(x, 0);
     if (x.timing) {
-      cudaEventRecord(evs[(size_t)s * NE + VEBI_NSTAGES], x.st);
-      used.emplace_back(x.ev_used, x.ev_used + VEBI_NSTAGES);
+      // read this step's stage events before the next step records them again
+      cudaEventSynchronize(x.ev[VEBI_NSTAGES]);
+      int prev = -1;
+      for (int q = 0; q <= VEBI_NSTAGES; ++q) {
+        bool u = q == VEBI_NSTAGES || x.ev_used[q];
+        if (!u) continue;
+        if (prev >= 0) {
+          float m = 0.f;
+          cudaEventElapsedTime(&m, x.ev[prev], x.ev[q]);
+          acc[prev] += m;
+        }
+        prev = q;
+      }
     }
   }
-  x.ev_run_step = -1;
   cudaEventRecord(e1, x.st);
   bool timing = x.timing;
-  x.timing = false;  // finish_step must not read the single-step events
+  x.timing = false;  // the stage sums are already collected
   int st = finish_step(x, last, true);
   x.timing = timing;
   float t = 0.f;
@@ -416,25 +465,8 @@ int vebi_run_steps(vebi_ctx* h, double x_mint, double y_mint, double x_maxt, dou
   if (ms) *ms = t;
   if (last) {
     last->nsteps = nsteps;
-    if (x.timing) {
-      for (int q = 0; q < VEBI_NSTAGES; ++q) last->stage_ms[q] = 0.0;
-      for (int s = 0; s < nsteps; ++s) {
-        int prev = -1;
-        for (int q = 0; q <= VEBI_NSTAGES; ++q) {
-          bool u = q == VEBI_NSTAGES || used[s][q];
-          if (!u) continue;
-          if (prev >= 0) {
-            float m = 0.f;
-            cudaEventElapsedTime(&m, evs[(size_t)s * NE + prev], evs[(size_t)s * NE + q]);
-            last->stage_ms[prev] += m;
-          }
-          prev = q;
-        }
-      }
-    }
+    for (int q = 0; q < VEBI_NSTAGES; ++q) last->stage_ms[q] = timing ? acc[q] : 0.0;
   }
-  for (auto& e : evs) cudaEventDestroy(e);
-  x.ev_run = nullptr;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return st;
@@ -473,6 +505,8 @@ int vebi_destroy(vebi_ctx* h) {
   if (!h) return VEBI_OK;
   Ctx& x = h->x;
   if (x.st) cudaStreamSynchronize(x.st);
+  for (auto& g : x.graph)
+    if (g) cudaGraphExecDestroy(g);
   for (void* p : x.allocs) cudaFree(p);
   x.allocs.clear();
   for (int i = 0; i <= VEBI_NSTAGES; ++i)
@@ -555,7 +589,7 @@ static DView dview(Ctx& x, const std::string& nm) {
   if (nm == "ushift_y") return D(d.ushy, n);
   if (nm == "ustar_x") return D(d.ux2, np);
   if (nm == "ustar_y") return D(d.uy2, np);
-  if (nm == "theta_star") return D(d.th, n);
+  if (nm == "theta_star") return D(d.th, n);  // theta* is the step's final theta
   if (nm == "ppe_B") return D(d.ppe_B, n);
   if (nm == "ppe_diag") return D(d.ppe_diag, n);
   if (nm == "ppe_val") return D(d.ppe_val, ell);

@@ -167,6 +167,16 @@ __device__ __forceinline__ void atomic_max_pos(unsigned long long* a, double v) 
 }
 __device__ __forceinline__ double bits_to_double(unsigned long long b) { return __longlong_as_double((long long)b); }
 
+// the same maximum with one atomic per warp; every lane of the warp must call it
+__device__ __forceinline__ void warp_max_pos(unsigned long long* a, double v) {
+  unsigned long long b = (v >= 0.0) ? (unsigned long long)__double_as_longlong(v) : 0ull;
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long q = __shfl_xor_sync(0xffffffffu, b, o);
+    b = q > b ? q : b;
+  }
+  if ((threadIdx.x & 31) == 0 && b) atomicMax(a, b);
+}
+
 __device__ __forceinline__ void set_error(Scal* s, int code) { atomicCAS(&s->error, 0, code); }
 
 // deterministic block sum: fixed shuffle tree, warps combined in order by warp 0

@@ -22,6 +22,11 @@ struct Ctx {
   bool ev_used[VEBI_NSTAGES]{};
   cudaEvent_t* ev_run = nullptr;   // per-step stage events of vebi_run_steps (timing on)
   int ev_run_step = -1;            // step whose events stage_mark records, -1 = use ev[]
+  bool capturing = false;          // enqueue_step is being captured into a CUDA graph
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one step: [0] plain, [1] with stage events
+  bool graph_failed[2] = {false, false};
+  int graph_launches[2] = {0, 0};
+  bool graph_used[2][VEBI_NSTAGES] = {};
   int coop_blocks = 0;       // persistent PPE grid (co-resident blocks)
   int gs_blocks = 0;         // grid of grid-stride kernels over dynamic counts
   int sel_max_blocks = 0;    // blocks of the ordered-select kernels
@@ -47,7 +52,8 @@ inline int grid_for(long long n, int tpb = TPB) {
 // stage timers: record the start event of stage `s` (ends at the next recorded stage)
 inline void stage_mark(Ctx& x, int s) {
   if (!x.timing) return;
-  if (x.ev_run_step >= 0) cudaEventRecord(x.ev_run[(size_t)x.ev_run_step * (VEBI_NSTAGES + 1) + s], x.st);
+  if (x.capturing) cudaEventRecordWithFlags(x.ev[s], x.st, cudaEventRecordExternal);
+  else if (x.ev_run_step >= 0) cudaEventRecord(x.ev_run[(size_t)x.ev_run_step * (VEBI_NSTAGES + 1) + s], x.st);
   else cudaEventRecord(x.ev[s], x.st);
   x.ev_used[s] = true;
 }

@@ -40,13 +40,16 @@ __global__ void k_step_reset(Scal* s, int npfb) {
 // STEP 1-2: keep r0,u0 and reduce max|u| over the fluid (set_time_step)
 __global__ void k_save_umax(Consts c, Dev d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= c.npfb) return;
-  double ux = d.ux[i], uy = d.uy[i];
-  d.r0x[i] = d.rx[i];
-  d.r0y[i] = d.ry[i];
-  d.u0x[i] = ux;
-  d.u0y[i] = uy;
-  if (i >= c.nbS) atomic_max_pos(&d.s->umax_bits, sqrt(ux * ux + uy * uy));
+  double um = -1.0;
+  if (i < c.npfb) {
+    double ux = d.ux[i], uy = d.uy[i];
+    d.r0x[i] = d.rx[i];
+    d.r0y[i] = d.ry[i];
+    d.u0x[i] = ux;
+    d.u0y[i] = uy;
+    if (i >= c.nbS) um = sqrt(ux * ux + uy * uy);
+  }
+  warp_max_pos(&d.s->umax_bits, um);
 }
 
 __device__ __forceinline__ double step_dt(const Consts& c, const Scal* s) {
@@ -56,16 +59,25 @@ __device__ __forceinline__ double step_dt(const Consts& c, const Scal* s) {
 }
 
 // STEP 3-4: advect, bin, replace escapees; per particle, in the reference's order
+__device__ __forceinline__ double advect_bin_one(const Consts& c, const Dev& d, int i, double dt);
+
 __global__ void k_advect_bin(Consts c, Dev d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= c.npfb) return;
   Scal* s = d.s;
   const double dt = step_dt(c, s);
   if (i == 0) s->dt = dt;
+  double um = -1.0;
   if (i < c.nbS) {  // walls do not move; they still enter the maximum of new_fick_shift
-    atomic_max_pos(&s->maxU_bits, sqrt(d.ux[i] * d.ux[i] + d.uy[i] * d.uy[i]));
-    return;
+    um = sqrt(d.ux[i] * d.ux[i] + d.uy[i] * d.uy[i]);
+  } else if (i < c.npfb) {
+    um = advect_bin_one(c, d, i, dt);
   }
+  warp_max_pos(&s->maxU_bits, um);
+}
+
+// one fluid particle: advection, put_in_bin, replace_escapees; returns |u| after binning
+__device__ __forceinline__ double advect_bin_one(const Consts& c, const Dev& d, int i, double dt) {
+  Scal* s = d.s;
   double x = d.r0x[i] + d.u0x[i] * dt;
   double y = d.r0y[i] + d.u0y[i] * dt;
   double ux = d.ux[i], uy = d.uy[i];
@@ -140,7 +152,7 @@ __global__ void k_advect_bin(Consts c, Dev d) {
   if (nesc) atomicAdd(&s->n_escapees, nesc);
   d.rx[i] = x;
   d.ry[i] = y;
-  atomic_max_pos(&s->maxU_bits, sqrt(ux * ux + uy * uy));
+  return sqrt(ux * ux + uy * uy);
 }
 
 // ------------------------------------------------------------------------------- mirrors
@@ -500,8 +512,7 @@ void launch_mirrors(Ctx& x) {
 
 // ------------------------------------------------------------------------------- mirror fields
 // mirror_velocities (mirror_boundaries_mod.F90:509-584): u* of mirrors from their parents' u*
-// (reads the new buffers ux2/uy2 of the predictor), then solid-parent copies.  Also carries
-// mirror theta into the new buffer.
+// (the predictor's output ux2/uy2), then solid-parent copies.
 __global__ void k_mirror_velocities(Consts c, Dev d) {
   const int nm = d.s->nmirror;
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nm; m += gridDim.x * blockDim.x) {
@@ -564,7 +575,6 @@ __global__ void k_mirror_velocities(Consts c, Dev d) {
     }
     d.ux2[j] = uj;
     d.uy2[j] = vj;
-    d.th2[j] = d.th[j];
   }
 }
 

@@ -31,13 +31,13 @@ __global__ void k_ppe_rhs(Consts c, Dev d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   double b = 0.0;
   if (i < c.npfb) {
-    const double ui = d.ux[i], vi = d.uy[i];
+    const double ui = d.ux2[i], vi = d.uy2[i];  // u* (predictor output, mirrors included)
     const double K11 = d.kgcm[0][i], K21 = d.kgcm[1][i], K12 = d.kgcm[2][i], K22 = d.kgcm[3][i];
     double fb = 0.0;
     const int cnt = d.ij_count[i];
     for (int k = 0; k < cnt; ++k) {
       int j = d.ij_link[ELL(k, i)];
-      double u1 = ui - d.ux[j], u2 = vi - d.uy[j];
+      double u1 = ui - d.ux2[j], u2 = vi - d.uy2[j];
       double w1 = d.wGx[ELL(k, i)], w2 = d.wGy[ELL(k, i)];
       double kw1 = K11 * w1 + K12 * w2, kw2 = K21 * w1 + K22 * w2;
       fb = fb - (u1 * kw1 + u2 * kw2);
@@ -50,10 +50,11 @@ __global__ void k_ppe_rhs(Consts c, Dev d) {
 }
 
 __global__ void k_ppe_mean(Consts c, Dev d, int nblk) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  __shared__ double sh[TPB / 32 + 1];
   double s = 0.0;
-  for (int b = 0; b < nblk; ++b) s += d.partials[b];
-  d.s->rhs_mean = (c.open_domain == 0) ? s / (double)c.npfb : 0.0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) s += d.partials[b];
+  s = block_sum<TPB>(s, sh);
+  if (threadIdx.x == 0) d.s->rhs_mean = (c.open_domain == 0) ? s / (double)c.npfb : 0.0;
 }
 
 // ---------------------------------------------------------------------- assembly
@@ -171,57 +172,65 @@ __device__ __forceinline__ void write_partials(double a, double b, int nval, dou
   __syncthreads();
 }
 
-__device__ __forceinline__ double spmv_row(const Consts& c, const int* __restrict__ cnt_,
-                                           const double* __restrict__ diag, const double* __restrict__ val,
-                                           const int* __restrict__ col, const double* xv, int i) {
-  double bb = __ldg(diag + i) * __ldcg(xv + i);
-  const int cnt = __ldg(cnt_ + i);
-  for (int k = 0; k < cnt; ++k) {
-    size_t e = ELL(k, i);
-    bb = fma(__ldg(val + e), __ldcg(xv + __ldg(col + e)), bb);
+// Solver arguments: only what the loop touches (keeps the kernel's register footprint small).
+struct BiArgs {
+  double *x, *r, *rb, *v, *p, *pinv, *s, *sinv, *t, *rinvM, *part, *P;
+  const double *B, *diag, *val;
+  const int *col, *cnt;
+  Scal* sc;
+  long long stride;
+  int n, itermax;
+  double tol;
+};
+
+// y_i = A_ii x_i + sum_k A_ik x_col(ik)  (sparse_atime, linear_solver.F90:254-273).  Two
+// interleaved accumulators keep two loads and two DFMAs in flight per thread; x was written
+// inside this kernel by other blocks, so it is read through L2 (ld.global.cg).
+__device__ __forceinline__ double spmv_row(const BiArgs& a, const double* xv, int i) {
+  const int cnt = __ldg(a.cnt + i);
+  const double* vp = a.val + i;
+  const int* cp = a.col + i;
+  const long long st = a.stride;
+  double b0 = __ldg(a.diag + i) * __ldcg(xv + i), b1 = 0.0;
+  int k = 0;
+  for (; k + 1 < cnt; k += 2) {
+    const int c0 = __ldg(cp), c1 = __ldg(cp + st);
+    const double v0 = __ldg(vp), v1 = __ldg(vp + st);
+    b0 = fma(v0, __ldcg(xv + c0), b0);
+    b1 = fma(v1, __ldcg(xv + c1), b1);
+    cp += 2 * st;
+    vp += 2 * st;
   }
-  return bb;
+  if (k < cnt) b0 = fma(__ldg(vp), __ldcg(xv + __ldg(cp)), b0);
+  return b0 + b1;
 }
 
+// SPARSE_PBICGSTAB_nonull (NONULL) / SPARSE_PBICGSTAB with x0 = 0.  The recurrences are the
+// reference's; the arithmetic uses fused multiply-adds and multiplies by 1/(M+1e-15) instead
+// of dividing by it (inverseM), which changes results by rounding only.
 template <bool NONULL>
-__global__ void __launch_bounds__(TPB) k_bicgstab(Consts c, Dev d) {
+__global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
   __shared__ double sh[64];
   __shared__ double shv[4];
-  const int n = c.npfb;
+  const int n = a.n;
   const int nb = gridDim.x;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int stride = gridDim.x * blockDim.x;
-  Scal* s = d.s;
-  double* part = d.partials;
-  double* __restrict__ x = d.bx;
-  double* __restrict__ r = d.br;
-  double* __restrict__ rb = d.brb;
-  double* __restrict__ v = d.bv;
-  double* __restrict__ p = d.bp;
-  double* __restrict__ pinv = d.bpi;
-  double* __restrict__ sv = d.bs;
-  double* __restrict__ sinv = d.bsi;
-  double* __restrict__ t = d.bt;
-  const double* __restrict__ Bv = d.ppe_B;
-  const double* __restrict__ diag = d.ppe_diag;
-  const double* __restrict__ val = d.ppe_val;
-  const int* __restrict__ col = d.ppe_col;
-  const int* __restrict__ cnt = d.ij_count;
-  const double tol = c.tol;
+  Scal* s = a.sc;
+  double* part = a.part;
+  const double rinv1 = 1.0 / (1.0 + 1.0e-15);
   const double small = NONULL ? 1.0e-6 : 4.0;  // open solver: the integer expression 10-6
-  // M: 1 (closed) or the diagonal (open); inverseM divides by M+1e-15
-  auto minv_den = [&](int i) -> double { return NONULL ? (1.0 + 1.0e-15) : (__ldg(diag + i) + 1.0e-15); };
   double red[2];
-  // initial guess x = 0: r = B - A*0 = B
   double acc = 0.0;
   for (int i = tid; i < n; i += stride) {
-    double bi = Bv[i];
-    x[i] = 0.0;
-    r[i] = bi;
-    rb[i] = bi;
-    v[i] = 0.0;
-    p[i] = 0.0;
-    acc += bi * bi;
+    double bi = a.B[i];
+    a.x[i] = 0.0;
+    a.r[i] = bi;
+    a.rb[i] = bi;
+    a.v[i] = 0.0;
+    a.p[i] = 0.0;
+    if (!NONULL) a.rinvM[i] = 1.0 / (__ldg(a.diag + i) + 1.0e-15);
+    acc = fma(bi, bi, acc);
   }
   // slot 10 for the initial reduction: slot 0 is rewritten before every block has read it
   write_partials(acc, 0.0, 1, part + 10 * (size_t)nb, sh);
@@ -231,37 +240,37 @@ __global__ void __launch_bounds__(TPB) k_bicgstab(Consts c, Dev d) {
   double n2r0 = 1.0, n2s0 = 1.0, resid = 0.0;
   int iter = 1, warn = 0;
   bool done = false;
-  while (iter <= c.itermax) {
+  while (iter <= a.itermax) {
     if (rho == 0.0) { warn |= VEBI_WARN_BICGSTAB_BREAKDOWN; done = true; break; }
     // p = r + beta (p - omega v)
-    double beta = rho / (rho0 + 1.0e-15) * alpha / (omega + 1.0e-15);
+    const double beta = rho / (rho0 + 1.0e-15) * alpha / (omega + 1.0e-15);
     acc = 0.0;
     for (int i = tid; i < n; i += stride) {
-      double pi = (iter == 1) ? r[i] : r[i] + beta * (p[i] - omega * v[i]);
-      p[i] = pi;
+      double pi = (iter == 1) ? a.r[i] : fma(beta, fma(-omega, a.v[i], a.p[i]), a.r[i]);
+      a.p[i] = pi;
       acc += pi;
     }
-    double* slot = part + 0 * (size_t)nb;
+    double* slot = part;
     if (NONULL) {
       write_partials(acc, 0.0, 1, slot, sh);
       if (!grid_sync(s)) return;
       reduce_partials(slot, nb, 1, red, shv);
       const double mean = red[0] / (double)n;
       for (int i = tid; i < n; i += stride) {
-        double pi = p[i] - mean;
-        p[i] = pi;
-        pinv[i] = pi / minv_den(i);
+        double pi = a.p[i] - mean;
+        a.p[i] = pi;
+        a.pinv[i] = pi * rinv1;
       }
     } else {
-      for (int i = tid; i < n; i += stride) pinv[i] = p[i] / minv_den(i);
+      for (int i = tid; i < n; i += stride) a.pinv[i] = a.p[i] * a.rinvM[i];
     }
     if (!grid_sync(s)) return;
     // v = A p_inv ; (r_bar, v)
     acc = 0.0;
     for (int i = tid; i < n; i += stride) {
-      double vi = spmv_row(c, cnt, diag, val, col, pinv, i);
-      v[i] = vi;
-      acc += rb[i] * vi;
+      double vi = spmv_row(a, a.pinv, i);
+      a.v[i] = vi;
+      acc = fma(a.rb[i], vi, acc);
     }
     slot = part + 2 * (size_t)nb;
     write_partials(acc, 0.0, 1, slot, sh);
@@ -272,9 +281,9 @@ __global__ void __launch_bounds__(TPB) k_bicgstab(Consts c, Dev d) {
     double a2 = 0.0;
     acc = 0.0;
     for (int i = tid; i < n; i += stride) {
-      double si = r[i] - alpha * v[i];
-      sv[i] = si;
-      acc += si * si;
+      double si = fma(-alpha, a.v[i], a.r[i]);
+      a.s[i] = si;
+      acc = fma(si, si, acc);
       a2 += si;
     }
     slot = part + 4 * (size_t)nb;
@@ -284,27 +293,27 @@ __global__ void __launch_bounds__(TPB) k_bicgstab(Consts c, Dev d) {
     const double n2s = red[0];
     const double mean_s = red[1] / (double)n;
     if (iter == 1) n2s0 = (n2s <= small) ? 1.0 : n2s;
-    if (n2s <= tol * tol * n2s0) {
-      for (int i = tid; i < n; i += stride) x[i] = x[i] + alpha * pinv[i];
+    if (n2s <= a.tol * a.tol * n2s0) {
+      for (int i = tid; i < n; i += stride) a.x[i] = fma(alpha, a.pinv[i], a.x[i]);
       resid = sqrt(n2s / n2s0);
       done = true;
       break;
     }
     // s -= mean (closed) ; s_inv
     for (int i = tid; i < n; i += stride) {
-      double si = sv[i];
-      if (NONULL) { si = si - mean_s; sv[i] = si; }
-      sinv[i] = si / minv_den(i);
+      double si = a.s[i];
+      if (NONULL) { si = si - mean_s; a.s[i] = si; }
+      a.sinv[i] = NONULL ? si * rinv1 : si * a.rinvM[i];
     }
     if (!grid_sync(s)) return;
     // t = A s_inv ; (t, s) ; |t|^2
     acc = 0.0;
     a2 = 0.0;
     for (int i = tid; i < n; i += stride) {
-      double ti = spmv_row(c, cnt, diag, val, col, sinv, i);
-      t[i] = ti;
-      acc += ti * sv[i];
-      a2 += ti * ti;
+      double ti = spmv_row(a, a.sinv, i);
+      a.t[i] = ti;
+      acc = fma(ti, a.s[i], acc);
+      a2 = fma(ti, ti, a2);
     }
     slot = part + 6 * (size_t)nb;
     write_partials(acc, a2, 2, slot, sh);
@@ -315,11 +324,11 @@ __global__ void __launch_bounds__(TPB) k_bicgstab(Consts c, Dev d) {
     acc = 0.0;
     a2 = 0.0;
     for (int i = tid; i < n; i += stride) {
-      x[i] = x[i] + alpha * pinv[i] + omega * sinv[i];
-      double ri = sv[i] - omega * t[i];
-      r[i] = ri;
-      acc += ri * ri;
-      a2 += rb[i] * ri;
+      a.x[i] = fma(omega, a.sinv[i], fma(alpha, a.pinv[i], a.x[i]));
+      double ri = fma(-omega, a.t[i], a.s[i]);
+      a.r[i] = ri;
+      acc = fma(ri, ri, acc);
+      a2 = fma(a.rb[i], ri, a2);
     }
     slot = part + 8 * (size_t)nb;
     write_partials(acc, a2, 2, slot, sh);
@@ -328,13 +337,13 @@ __global__ void __launch_bounds__(TPB) k_bicgstab(Consts c, Dev d) {
     const double n2r = red[0];
     if (iter == 1) n2r0 = (n2r <= small) ? 1.0 : n2r;
     resid = sqrt(n2r / n2r0);
-    if (n2r <= tol * tol * n2r0) { done = true; break; }
+    if (n2r <= a.tol * a.tol * n2r0) { done = true; break; }
     iter = iter + 1;
     rho0 = rho;
     rho = red[1];
   }
   if (!done) warn |= VEBI_WARN_MAXITER;
-  for (int i = tid; i < n; i += stride) d.p[i] = x[i];
+  for (int i = tid; i < n; i += stride) a.P[i] = a.x[i];
   if (tid == 0) {
     s->ls_iters = iter;
     s->ls_iters_total += iter;
@@ -359,7 +368,7 @@ void launch_ppe(Ctx& x) {
   int g = grid_for(c.npfb);
   stage_mark(x, 9);
   VEBI_LAUNCH(x, k_ppe_rhs, g, TPB, c, x.d);
-  VEBI_LAUNCH(x, k_ppe_mean, 1, 32, c, x.d, g);
+  VEBI_LAUNCH(x, k_ppe_mean, 1, TPB, c, x.d, g);
   VEBI_LAUNCH(x, k_ppe_assemble, g, TPB, c, x.d);
   stage_mark(x, 10);
   // persistent cooperative launch: all blocks co-resident, so the grid barrier is safe
@@ -376,8 +385,11 @@ void launch_ppe(Ctx& x) {
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (c.open_domain == 0) cudaLaunchKernelEx(&cfg, k_bicgstab<true>, c, x.d);
-  else cudaLaunchKernelEx(&cfg, k_bicgstab<false>, c, x.d);
+  const Dev& d = x.d;
+  BiArgs a{d.bx, d.br, d.brb, d.bv, d.bp, d.bpi, d.bs, d.bsi, d.bt, d.bM, d.partials, d.p,
+           d.ppe_B, d.ppe_diag, d.ppe_val, d.ppe_col, d.ij_count, d.s, (long long)c.npfb, c.npfb, c.itermax, c.tol};
+  if (c.open_domain == 0) cudaLaunchKernelEx(&cfg, k_bicgstab<true>, a);
+  else cudaLaunchKernelEx(&cfg, k_bicgstab<false>, a);
   x.launches++;
 }
 

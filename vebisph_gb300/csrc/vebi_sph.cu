@@ -337,12 +337,8 @@ __global__ void k_predictor(Consts c, Dev d) {
   }
 }
 
-// ---------------------------------------------------------------------- pressure gradient
-// grad P, velocity update (div_free.F90:96-101), final advection (:111-117); reads the
-// current buffers (u*) and writes u^{n+1}, r^{n+1} into the second buffers.
-__global__ void k_pgrad_final(Consts c, Dev d) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= c.npfb) return;
+__device__ __forceinline__ void pgrad_one(const Consts& c, const Dev& d, int i, double& mu, double& mv,
+                                          double& mp) {
   const double pi_ = d.p[i];
   double a = 0, b = 0;
   const int cnt = d.ij_count[i];
@@ -357,7 +353,7 @@ __global__ void k_pgrad_final(Consts c, Dev d) {
   d.gpx[i] = gx;
   d.gpy[i] = gy;
   const double dt = d.s->dt;
-  double ux = d.ux[i], uy = d.uy[i], x = d.rx[i], y = d.ry[i];
+  double ux = d.ux2[i], uy = d.uy2[i], x = d.rx[i], y = d.ry[i];
   if (i >= c.nbS) {
     ux = ux + dt * (c.bf[0] - gx);
     uy = uy + dt * (c.bf[1] - gy);
@@ -368,14 +364,27 @@ __global__ void k_pgrad_final(Consts c, Dev d) {
     x = d.r0x[i] + 0.5 * (ux + d.u0x[i]) * dt + d.ushx[i] * dt;
     y = d.r0y[i] + 0.5 * (uy + d.u0y[i]) * dt + d.ushy[i] * dt;
   }
-  d.ux2[i] = ux;
-  d.uy2[i] = uy;
-  d.rx2[i] = x;
-  d.ry2[i] = y;
-  atomic_max_pos(&d.s->absu_bits, fabs(ux));
-  atomic_max_pos(&d.s->absv_bits, fabs(uy));
-  atomic_max_pos(&d.s->absp_bits, fabs(pi_));
+  d.ux[i] = ux;
+  d.uy[i] = uy;
+  d.rx[i] = x;
+  d.ry[i] = y;
+  mu = fabs(ux);
+  mv = fabs(uy);
+  mp = fabs(pi_);
 }
+
+// ---------------------------------------------------------------------- pressure gradient
+// grad P, velocity update (div_free.F90:96-101), final advection (:111-117): reads u* (ux2)
+// and writes u^{n+1} and r^{n+1} in place (no kernel of this launch reads neighbours' u or r).
+__global__ void k_pgrad_final(Consts c, Dev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double mu = -1.0, mv = -1.0, mp = -1.0;
+  if (i < c.npfb) pgrad_one(c, d, i, mu, mv, mp);
+  warp_max_pos(&d.s->absu_bits, mu);
+  warp_max_pos(&d.s->absv_bits, mv);
+  warp_max_pos(&d.s->absp_bits, mp);
+}
+
 
 // secondary_properties: vorticity from final fluid u and mirror u* (div_free.F90:160-183)
 __global__ void k_secondary(Consts c, Dev d, const double* __restrict__ uxn, const double* __restrict__ uyn,
@@ -401,10 +410,11 @@ __global__ void k_secondary(Consts c, Dev d, const double* __restrict__ uxn, con
 }
 
 __global__ void k_secondary_final(Consts c, Dev d, int nblk) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  __shared__ double sh[TPB / 32 + 1];
   double s = 0.0;
-  for (int b = 0; b < nblk; ++b) s += d.partials[b];
-  d.s->rms_u = sqrt(s / (double)c.npfb);
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) s += d.partials[b];
+  s = block_sum<TPB>(s, sh);
+  if (threadIdx.x == 0) d.s->rms_u = sqrt(s / (double)c.npfb);
 }
 
 void launch_weights_surface_shift(Ctx& x) {
@@ -442,10 +452,8 @@ void launch_predictor(Ctx& x) {
   stage_mark(x, 8);
   VEBI_LAUNCH(x, k_predictor, g, TPB, c, x.d);
   launch_mirror_velocities(x);
-  // u*, theta* become the current buffers
-  std::swap(x.d.ux, x.d.ux2);
-  std::swap(x.d.uy, x.d.uy2);
-  std::swap(x.d.th, x.d.th2);
+  // theta* replaces theta for walls and fluid; u* stays in ux2/uy2 for the PPE and the update
+  cudaMemcpyAsync(x.d.th, x.d.th2, sizeof(double) * (size_t)c.npfb, cudaMemcpyDeviceToDevice, x.st);
 }
 
 void launch_final(Ctx& x, int secondary) {
@@ -453,16 +461,14 @@ void launch_final(Ctx& x, int secondary) {
   int g = grid_for(c.npfb);
   stage_mark(x, 11);
   launch_mirror_pressure(x);
+  // keep r* (fluid and mirrors) readable after the step: the update below overwrites r
+  cudaMemcpyAsync(x.d.rx2, x.d.rx, sizeof(double) * (size_t)c.cap, cudaMemcpyDeviceToDevice, x.st);
+  cudaMemcpyAsync(x.d.ry2, x.d.ry, sizeof(double) * (size_t)c.cap, cudaMemcpyDeviceToDevice, x.st);
   VEBI_LAUNCH(x, k_pgrad_final, g, TPB, c, x.d);
-  // u^{n+1}, r^{n+1} become current; u*, r* stay in the second buffers
-  std::swap(x.d.ux, x.d.ux2);
-  std::swap(x.d.uy, x.d.uy2);
-  std::swap(x.d.rx, x.d.rx2);
-  std::swap(x.d.ry, x.d.ry2);
   if (secondary) {
     stage_mark(x, 13);
     VEBI_LAUNCH(x, k_secondary, g, TPB, c, x.d, x.d.ux, x.d.uy, x.d.ux2, x.d.uy2);
-    VEBI_LAUNCH(x, k_secondary_final, 1, 32, c, x.d, g);
+    VEBI_LAUNCH(x, k_secondary_final, 1, TPB, c, x.d, g);
   }
 }
 
