@@ -101,7 +101,9 @@ typedef struct vebi_params {
   int32_t nplink;                      /* neighbour / cell capacity; the reference uses 75       */
   int32_t nmirror_cap;                 /* mirror capacity; 0 = reference estimate 2*npfb         */
   int32_t precision;                   /* VEBI_PREC_*                                            */
-  int32_t reserved[7];
+  int32_t correct_velocity;            /* 1: run correct_velocity after the update; the reference
+                                          has the call commented out (div_free.F90:105)          */
+  int32_t reserved[6];
 } vebi_params;
 
 /* Per-step scalars the Fortran driver and `output` read after div_free

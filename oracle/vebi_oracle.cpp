@@ -1318,6 +1318,36 @@ struct Oracle {
     }
   }
 
+  // correct_velocity (correct_velocity.F90:13-70): remove the velocity component of particles
+  // closing on a wall mirror closer than dx.  The reference indexes b_type(vrelation(j)) also for
+  // circle mirrors (vrelation = 999+ib, out of range); here a circle mirror is not a wall.
+  void correct_velocity() {
+    std::vector<int> close(npfb, -1);
+    for (int i = nbS; i < npfb; ++i) {
+      double r_min2 = dx * dx;
+      for (int k = 0; k < ij_count[i]; ++k) {
+        int j = L(k, i);
+        if (j < npfb) continue;
+        double a = rx[i] - rx[j], b = ry[i] - ry[j];
+        double d2 = a * a + b * b;
+        if (!(d2 < r_min2)) continue;
+        int vr = vrelation[j];
+        if (vr > 0 && vr < 999 && P.b_type[vr - 1] == 1) { r_min2 = d2; close[i] = j; }
+        if (vr == -1 || vr < -2) { r_min2 = d2; close[i] = j; }
+      }
+    }
+    for (int i = nbS; i < npfb; ++i) {
+      int j = close[i];
+      if (j < 0) continue;
+      double n1 = rx[i] - rx[j], n2 = ry[i] - ry[j];
+      double t = std::sqrt(n1 * n1 + n2 * n2);
+      n1 = n1 / t; n2 = n2 / t;
+      double u1 = ux[i] - ux[j], u2 = uy[i] - uy[j];
+      double un = u1 * n1 + u2 * n2;
+      if (un <= 0.0) { ux[i] = ux[i] - un * n1; uy[i] = uy[i] - un * n2; }
+    }
+  }
+
   // secondary_properties (div_free.F90:148-192), only when asked
   void secondary_properties() {
 #pragma omp parallel for schedule(static)
@@ -1411,6 +1441,8 @@ struct Oracle {
         uy[i] = u0y[i] + dt * P.body_force[1];
       }
     }
+    // STEP 10 (off in the reference: the call is commented out, div_free.F90:105)
+    if (P.correct_velocity) correct_velocity();
     // STEP 11
     mark(13);
     if (secondary) secondary_properties();

@@ -15,7 +15,15 @@ CASES = {
     "cylinder20k": lambda: cases.cylinder(2.0e4, Wi=0.6, seed=2),
     "cavity64": lambda: cases.cavity(64, seed=3),
     "poiseuille_newtonian": lambda: cases.poiseuille(32, seed=4, const_mod=1),
+    "free_surface_open": lambda: cases.free_surface_periodic(75, seed=5),
+    "poiseuille_correct_velocity": lambda: _with(cases.poiseuille(40, seed=6), correct_velocity=1),
 }
+
+
+def _with(case, **kw):
+    for k, v in kw.items():
+        setattr(case, k, v)
+    return case
 
 
 @pytest.fixture(scope="module")
@@ -39,6 +47,11 @@ def test_one_step_parity(libs, name):
     rep = compare_step(gpu, ref, case)
     bad = failures(rep)
     assert not bad, bad
+    if case.i_open_domain == 1:  # free-surface identification (freesurf_mod.F90:17-68)
+        assert np.array_equal(gpu.get("n_surf")[: case.npfb], ref.get("n_surf")[: case.npfb])
+        for nm in ("conc", "div_r"):
+            a, b = gpu.get(nm), ref.get(nm)
+            assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max(), nm
     # vorticity diagnostic (secondary_properties) follows the final velocity
     v_g, v_o = gpu.get("vort"), ref.get("vort")
     assert np.abs(v_g - v_o).max() <= 1e-5 * max(np.abs(v_o).max(), 1e-30)

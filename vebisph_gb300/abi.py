@@ -56,8 +56,8 @@ class VebiParams(C.Structure):
         ("i_open_domain", C.c_int32), ("i_shift_coeff", C.c_int32),
         ("npfb", C.c_int32), ("nbS", C.c_int32),
         ("const_mod", C.c_int32), ("itermax", C.c_int32), ("nplink", C.c_int32),
-        ("nmirror_cap", C.c_int32), ("precision", C.c_int32),
-        ("reserved", C.c_int32 * 7),
+        ("nmirror_cap", C.c_int32), ("precision", C.c_int32), ("correct_velocity", C.c_int32),
+        ("reserved", C.c_int32 * 6),
     ]
 
 

@@ -67,6 +67,7 @@ class Case:
     itermax: int = 1000
     nplink: int = 75
     nmirror_cap: int = 0
+    correct_velocity: int = 0
 
     def __post_init__(self):
         n = self.npfb
@@ -133,6 +134,7 @@ class Case:
         p.nplink = self.nplink
         p.nmirror_cap = self.nmirror_cap
         p.precision = precision
+        p.correct_velocity = self.correct_velocity
         return p
 
     def fortran_planes(self, ld: int | None = None) -> dict:
@@ -419,6 +421,42 @@ def cavity(n: int = 1024, seed: int = 0, Ra: float = 1.0e5, Pr: float = 1.0, Wi:
                 dv=dx * dx, Ra=Ra, Pr=Pr, El=Wi / Re, beta=beta, body_force=(0.0, 0.0),
                 ve_nonlinearity=0.0, b_node=b_node, b_edge=b_edge, b_type=b_type, b_vel=b_vel,
                 b_thermal=b_th, b_periodic_parent=np.zeros(4, int))
+
+
+def free_surface_periodic(n: int = 75, seed: int | None = None) -> Case:
+    """Open-domain case: datclass case 8 "FREE SURFACE PERIODIC" (datclass.F90:561-631) --
+    a 2x2 box, wall at y=0, periodic in x, no boundary on top (b_type 0), fluid filling
+    y < 1, i_open_domain=1, shift_coeff=1, PTT with ve_nonlinearity=400, beta=0.1, Ra=1e3,
+    Pr=10, El=1, dx = 2/n.  seed=None gives the unjittered lattice of the generator."""
+    xl = yl = 2.0
+    dx = yl / n
+    h = 1.3 * dx
+    b_node = np.array([[0.0, 0.0], [xl, 0.0], [xl, yl], [0.0, yl]])
+    b_edge = make_boundary_edge_vectors(b_node)
+    b_type = np.array([1, 2, 0, 2])
+    b_vel = np.array([-0.0, 0.0, 0.0, 0.0])
+    b_th = np.array([1.0, 0.0, -1.0, 0.0])
+    xs, ys, us, vs, ths = make_boundary_particles(b_node, b_edge, b_type, b_vel, b_th, dx)
+    fx, fy, ft = [], [], []
+    x = 0.0 + 0.5 * dx
+    while x < xl:
+        y = 0.0 + dx
+        while y < 0.5 * yl:
+            fx.append(x)
+            fy.append(y)
+            ft.append(1.0 if y <= 0.125 * yl + 0.0625 * yl * math.sin(2.0 * PI * x) else -1.0)
+            y = y + dx
+        x = x + dx
+    fr = np.stack([fx, fy], 1)
+    if seed is not None:
+        fr += _jitter(np.random.default_rng(seed), len(fr), dx)
+    r = np.concatenate([np.stack([xs, ys], 1), fr])
+    u = np.zeros_like(r)
+    theta = np.concatenate([ths, ft])
+    return Case(name=f"free_surface_periodic_{n}", r=r, u=u, theta=theta, npfb=len(r), nbS=len(xs), h=h, dx=dx,
+                dv=dx * dx, Ra=1000.0, Pr=10.0, El=1.0, beta=0.1, body_force=(0.0, 0.0), ve_nonlinearity=400.0,
+                i_open_domain=1, i_shift_coeff=1, b_node=b_node, b_edge=b_edge, b_type=b_type, b_vel=b_vel,
+                b_thermal=b_th, b_periodic_parent=np.array([0, 4, 0, 2]))
 
 
 def by_name(name: str, **kw) -> Case:

@@ -11,6 +11,7 @@
 namespace vebi {
 
 int ppe_solver_blocks(int device, int nsm);
+int ppe_mixed_blocks(int nsm);
 
 static thread_local std::string g_err;
 
@@ -90,6 +91,7 @@ static int build_consts(Ctx& x) {
   c.coeff_polymeric = (1.0 - P.beta) * P.Pr / (P.Ra * P.El);
   c.coeff_theta = 1.0 / std::sqrt(P.Ra * P.Pr);
   c.wab1 = host_wab(c.ad_7, c.dx / c.h);
+  c.cell_size = 1.0 / c.uno_sup_size;
   c.tol = P.tol > 0 ? P.tol : 1.0e-8;
   c.itermax = P.itermax > 0 ? P.itermax : 1000;
   c.nplink = P.nplink > 0 ? P.nplink : 75;
@@ -97,6 +99,7 @@ static int build_consts(Ctx& x) {
   c.open_domain = P.i_open_domain;
   c.shift_coeff = P.i_shift_coeff;
   c.const_mod = P.const_mod == 1 ? 1 : 2;
+  c.correct_velocity = P.correct_velocity ? 1 : 0;
   c.npfb = P.npfb;
   c.nbS = P.nbS;
   for (int i = 0; i < nb; ++i) {
@@ -204,6 +207,7 @@ static int allocate_all(Ctx& x) {
   A_(d.scan_part, (size_t)c.nct / 1024 + 2);
   size_t sel_items = (size_t)(c.npfb > c.mcap ? c.npfb : c.mcap);
   A_(d.sel_blk, sel_items / SEL_CH + 2);
+  A_(d.pk, cap);
   A_(d.ij_count, n); A_(d.ij_link, E);
   A_(d.wGx, E); A_(d.wGy, E); A_(d.wL, E);
   for (int q = 0; q < 4; ++q) A_(d.kgcm[q], n);
@@ -220,6 +224,11 @@ static int allocate_all(Ctx& x) {
   size_t coop_part = (size_t)x.coop_blocks * 12;
   A_(d.partials, (np_part > coop_part ? np_part : coop_part) + 64);
   A_(d.gpx, n); A_(d.gpy, n);
+  if (x.precision == VEBI_PREC_MIXED) {
+    A_(d.ppe_val32, E); A_(d.rowsum, n); A_(d.pi2, n); A_(d.si2, n);
+    A_(d.wGx32, E); A_(d.wGy32, E); A_(d.wL32, E);
+    for (int q = 0; q < 4; ++q) A_(d.kgcm32[q], n);
+  }
 #undef A_
   return VEBI_OK;
 }
@@ -257,6 +266,8 @@ int vebi_create(const vebi_params* params, vebi_ctx** out) {
   cudaGetDevice(&x.device);
   cudaDeviceGetAttribute(&x.nsm, cudaDevAttrMultiProcessorCount, x.device);
   x.coop_blocks = ppe_solver_blocks(x.device, x.nsm);
+  x.coop_blocks_mixed = ppe_mixed_blocks(x.nsm);
+  if (x.coop_blocks_mixed > x.coop_blocks) x.coop_blocks = x.coop_blocks_mixed;  // partials sizing
   x.gs_blocks = x.nsm * 8;
   if (cudaStreamCreateWithFlags(&x.st, cudaStreamNonBlocking) != cudaSuccess) {
     delete h;
@@ -573,6 +584,8 @@ static DView dview(Ctx& x, const std::string& nm) {
   if (nm == "w_Gx") return D(d.wGx, ell);
   if (nm == "w_Gy") return D(d.wGy, ell);
   if (nm == "w_L") return D(d.wL, ell);
+  if (nm == "w_L32" && d.wL32) return DView{d.wL32, 4, ell};
+  if (nm == "w_Gx32" && d.wGx32) return DView{d.wGx32, 4, ell};
   if (nm == "kgcm11") return D(d.kgcm[0], n);
   if (nm == "kgcm21") return D(d.kgcm[1], n);
   if (nm == "kgcm12") return D(d.kgcm[2], n);

@@ -158,13 +158,40 @@ __global__ void k_cell_sort(Consts c, Dev d) {
   }
 }
 
-// pair list: thread per particle, cells in the reference's order, FP64 test 0 < r^2 <= 9h^2
+// FP32 offset of each particle to its cell origin, plus its cell coordinates (as floats):
+// pair offsets then need no large coordinate subtracted in FP32
+__global__ void k_cell_offsets(Consts c, Dev d) {
+  const int np = d.s->np;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < np; k += gridDim.x * blockDim.x) {
+    int key = d.cellpart[k];
+    float4 v = make_float4(0.f, 0.f, -1.0e6f, -1.0e6f);
+    if (key >= 0) {
+      int cx = key % c.ncx, cy = key / c.ncx;
+      double ox = (d.rx[k] - c.x_mint) - (double)cx * c.cell_size;
+      double oy = (d.ry[k] - c.y_mint) - (double)cy * c.cell_size;
+      v = make_float4((float)ox, (float)oy, (float)cx, (float)cy);
+    }
+    d.pk[k] = v;
+  }
+}
+
+// pair list: thread per particle, cells in the reference's order, test 0 < r^2 <= 9h^2.
+// The test is decided in FP32 from the cell-relative offsets when it is far from both
+// thresholds, and in FP64 on the reference's expression otherwise.  Error bound of the FP32
+// r^2: offsets are < S (the cell edge) with error <= eps S, the pair offset |r| < 2S gathers
+// at most ~6 eps S, so |r^2_32 - r^2| < ~32 eps S^2 = 32 eps sup_size_2; the band below is
+// 64 eps sup_size_2 (eps = 2^-24), so every pair inside it is re-tested exactly and the list
+// equals the FP64 list.
 __global__ void k_neighbours(Consts c, Dev d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.npfb) return;
   int cnt = 0;
   if (!d.inbin[i] && d.cellpart[i] >= 0) {
     const double xi = d.rx[i], yi = d.ry[i];
+    const float4 pi = d.pk[i];
+    const float S = (float)c.cell_size;
+    const float S2 = (float)c.sup_size_2;
+    const float band = 64.0f * 5.9604645e-8f * S2;
     const int ic = d.cellpart[i] + 1;  // 1-based as the reference
     const int icx = ic % c.ncx;        // the reference's column formula: last column -> 0
     const int icy = ic / c.ncx + 1;
@@ -191,9 +218,18 @@ __global__ void k_neighbours(Consts c, Dev d) {
       int s0 = d.cell_start[cc], s1 = s0 + d.cell_cnt[cc];
       for (int jj = s0; jj < s1; ++jj) {
         int j = d.ip[jj];
-        double r1 = xi - d.rx[j], r2 = yi - d.ry[j];
-        double rr2 = r1 * r1 + r2 * r2;
-        if (rr2 > 0.0 && rr2 <= c.sup_size_2) {
+        const float4 pj = d.pk[j];
+        const float f1 = (pi.x - pj.x) + (pi.z - pj.z) * S, f2 = (pi.y - pj.y) + (pi.w - pj.w) * S;
+        const float q = fmaf(f1, f1, f2 * f2);
+        bool take;
+        if (q > S2 + band) take = false;
+        else if (q < S2 - band && q > band) take = true;
+        else {  // near a threshold: the reference's FP64 test
+          double r1 = xi - d.rx[j], r2 = yi - d.ry[j];
+          double rr2 = r1 * r1 + r2 * r2;
+          take = rr2 > 0.0 && rr2 <= c.sup_size_2;
+        }
+        if (take) {
           if (cnt < c.nplink) d.ij_link[(size_t)cnt * c.npfb + i] = j;
           else over = true;
           ++cnt;
@@ -219,6 +255,7 @@ void launch_cells_neighbours(Ctx& x) {
   VEBI_LAUNCH(x, k_scan_apply, nblk, TPB, c, x.d);
   VEBI_LAUNCH(x, k_scatter, x.gs_blocks, TPB, x.d);
   VEBI_LAUNCH(x, k_cell_sort, grid_for((long long)c.nct * 32), TPB, c, x.d);
+  VEBI_LAUNCH(x, k_cell_offsets, x.gs_blocks, TPB, c, x.d);
   stage_mark(x, 3);
   VEBI_LAUNCH(x, k_neighbours, grid_for(c.npfb), TPB, c, x.d);
 }

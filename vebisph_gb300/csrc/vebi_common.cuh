@@ -26,6 +26,7 @@ struct Consts {
   double dt_coef_cfl, dt_coef_visc, dt_visc;
   double coeff_solvent, coeff_polymeric, coeff_theta;
   double wab1;                                      // Wab(dx/h) of shifting_forces
+  double cell_size;                                 // 1/uno_sup_size: edge of a cell
   double tol;
   // boundary framework (IBOUND)
   double b_node[VEBI_MAX_PATCHES][2], b_edge[VEBI_MAX_PATCHES][2];
@@ -40,6 +41,7 @@ struct Consts {
   int ncx, ncy, nct;
   int npfb, nbS, cap, mcap, nplink;
   int open_domain, shift_coeff, const_mod, itermax;
+  int correct_velocity;                             // run correct_velocity (off in the reference)
 };
 
 // Scalars that change during a step; they live in device memory so no step needs a host sync.
@@ -103,7 +105,12 @@ struct Dev {
   double* red;                               // small reduction scratch
   double *gpx, *gpy;
   // mixed precision
-  float *ppe_val32, *f32a, *f32b;
+  float* ppe_val32;                          // FP32 off-diagonal values
+  double* rowsum;                            // FP64 row sums of the PPE matrix
+  float2 *pi2, *si2;                         // p_inv, s_inv as FP32 (hi, lo) pairs
+  float4* pk;                                // FP32 offset to the cell origin + cell coords
+  float *wGx32, *wGy32, *wL32;               // FP32 pair weights (ELL)
+  float* kgcm32[4];
 };
 
 // ---------------------------------------------------------------------------------------------

@@ -28,6 +28,7 @@ struct Ctx {
   int graph_launches[2] = {0, 0};
   bool graph_used[2][VEBI_NSTAGES] = {};
   int coop_blocks = 0;       // persistent PPE grid (co-resident blocks)
+  int coop_blocks_mixed = 0; // same for the mixed-precision solver
   int gs_blocks = 0;         // grid of grid-stride kernels over dynamic counts
   int sel_max_blocks = 0;    // blocks of the ordered-select kernels
   int precision = VEBI_PREC_FP64;

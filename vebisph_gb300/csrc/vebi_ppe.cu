@@ -58,7 +58,7 @@ __global__ void k_ppe_mean(Consts c, Dev d, int nblk) {
 }
 
 // ---------------------------------------------------------------------- assembly
-__global__ void k_ppe_assemble(Consts c, Dev d) {
+__global__ void k_ppe_assemble(Consts c, Dev d, const float* __restrict__ wL32) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.npfb) return;
   double B = d.ppe_B[i];
@@ -75,7 +75,8 @@ __global__ void k_ppe_assemble(Consts c, Dev d) {
   double Adiag = 0.0;
   for (int k = 0; k < cnt; ++k) {
     int j = d.ij_link[ELL(k, i)];
-    double temp = -d.wL[ELL(k, i)];
+    // the mixed step assembles in FP64 from its FP32 Morris weights
+    double temp = wL32 ? -(double)wL32[ELL(k, i)] : -d.wL[ELL(k, i)];
     Adiag = Adiag - temp;
     int colk = j;
     bool self = false;
@@ -183,26 +184,35 @@ struct BiArgs {
   double tol;
 };
 
-// y_i = A_ii x_i + sum_k A_ik x_col(ik)  (sparse_atime, linear_solver.F90:254-273).  Two
-// interleaved accumulators keep two loads and two DFMAs in flight per thread; x was written
-// inside this kernel by other blocks, so it is read through L2 (ld.global.cg).
+// y_i = A_ii x_i + sum_k A_ik x_col(ik)  (sparse_atime, linear_solver.F90:254-273).  Four
+// interleaved accumulators keep four independent load chains (column -> x) in flight per thread.
+// x was written inside this kernel by other blocks: the grid barrier's release/acquire fences
+// (gpu scope, followed by a CTA barrier) make those writes visible to the L1-cached loads
+// (ld.global.ca) that follow, as in a cooperative-groups grid sync; neighbouring rows share most
+// of their columns, so the gathers mostly hit L1.
 __device__ __forceinline__ double spmv_row(const BiArgs& a, const double* xv, int i) {
   const int cnt = __ldg(a.cnt + i);
   const double* vp = a.val + i;
   const int* cp = a.col + i;
   const long long st = a.stride;
-  double b0 = __ldg(a.diag + i) * __ldcg(xv + i), b1 = 0.0;
+  double b0 = __ldg(a.diag + i) * __ldca(xv + i), b1 = 0.0, b2 = 0.0, b3 = 0.0;
   int k = 0;
-  for (; k + 1 < cnt; k += 2) {
-    const int c0 = __ldg(cp), c1 = __ldg(cp + st);
-    const double v0 = __ldg(vp), v1 = __ldg(vp + st);
-    b0 = fma(v0, __ldcg(xv + c0), b0);
-    b1 = fma(v1, __ldcg(xv + c1), b1);
-    cp += 2 * st;
-    vp += 2 * st;
+  for (; k + 3 < cnt; k += 4) {
+    const int c0 = __ldg(cp), c1 = __ldg(cp + st), c2 = __ldg(cp + 2 * st), c3 = __ldg(cp + 3 * st);
+    const double v0 = __ldg(vp), v1 = __ldg(vp + st), v2 = __ldg(vp + 2 * st), v3 = __ldg(vp + 3 * st);
+    b0 = fma(v0, __ldca(xv + c0), b0);
+    b1 = fma(v1, __ldca(xv + c1), b1);
+    b2 = fma(v2, __ldca(xv + c2), b2);
+    b3 = fma(v3, __ldca(xv + c3), b3);
+    cp += 4 * st;
+    vp += 4 * st;
   }
-  if (k < cnt) b0 = fma(__ldg(vp), __ldcg(xv + __ldg(cp)), b0);
-  return b0 + b1;
+  for (; k < cnt; ++k) {
+    b0 = fma(__ldg(vp), __ldca(xv + __ldg(cp)), b0);
+    cp += st;
+    vp += st;
+  }
+  return (b0 + b1) + (b2 + b3);
 }
 
 // SPARSE_PBICGSTAB_nonull (NONULL) / SPARSE_PBICGSTAB with x0 = 0.  The recurrences are the
@@ -363,14 +373,23 @@ int ppe_solver_blocks(int device, int nsm) {
   return per * nsm;
 }
 
+void launch_ppe_mixed_solve(Ctx& x);
+void launch_ppe_rhs32(Ctx& x);
+
 void launch_ppe(Ctx& x) {
   const Consts& c = x.c;
   int g = grid_for(c.npfb);
   stage_mark(x, 9);
-  VEBI_LAUNCH(x, k_ppe_rhs, g, TPB, c, x.d);
+  const bool mixed = x.precision == VEBI_PREC_MIXED;
+  if (mixed) launch_ppe_rhs32(x);
+  else VEBI_LAUNCH(x, k_ppe_rhs, g, TPB, c, x.d);
   VEBI_LAUNCH(x, k_ppe_mean, 1, TPB, c, x.d, g);
-  VEBI_LAUNCH(x, k_ppe_assemble, g, TPB, c, x.d);
+  VEBI_LAUNCH(x, k_ppe_assemble, g, TPB, c, x.d, mixed ? (const float*)x.d.wL32 : (const float*)nullptr);
   stage_mark(x, 10);
+  if (x.precision == VEBI_PREC_MIXED) {
+    launch_ppe_mixed_solve(x);
+    return;
+  }
   // persistent cooperative launch: all blocks co-resident, so the grid barrier is safe
   int nblk = x.coop_blocks;
   long long need = (c.npfb + TPB - 1) / TPB;
@@ -390,6 +409,248 @@ void launch_ppe(Ctx& x) {
            d.ppe_B, d.ppe_diag, d.ppe_val, d.ppe_col, d.ij_count, d.s, (long long)c.npfb, c.npfb, c.itermax, c.tol};
   if (c.open_domain == 0) cudaLaunchKernelEx(&cfg, k_bicgstab<true>, a);
   else cudaLaunchKernelEx(&cfg, k_bicgstab<false>, a);
+  x.launches++;
+}
+
+}  // namespace vebi
+
+// =====================================================================================
+// Mixed precision PPE (VEBI_PREC_MIXED): the BiCGSTAB of the FP64 step with an FP32 SpMV.
+//
+// FP32 Krylov recurrences cannot solve this system at scale: the attainable relative residual
+// of a Krylov method is ~ eps * cond(A), and the Laplacian of a 4M-particle domain has
+// cond ~ 1e7, so FP32 (eps 6e-8) stalls near 1 (an FP32 inner solver inside FP64 refinement
+// diverged on the 4M cylinder).  The recurrences, dot products and the solution therefore stay
+// FP64, and the SpMV -- the bytes and the FP64 instructions of the solve -- runs in FP32 in the
+// Laplacian's difference form
+//     y_i = rowsum_i * x_i + sum_k A_ik (x_col(ik) - x_i),       rowsum_i = A_ii + sum_k A_ik,
+// with rowsum in FP64 (0 up to rounding except Dirichlet rows) and the sum in FP32.  The
+// vectors the SpMV gathers (p_inv, s_inv) are kept as FP32 hi/lo pairs (x = hi + lo), so
+// x_j - x_i = (hi_j - hi_i) + (lo_j - lo_i) keeps FP32 accuracy relative to the difference
+// instead of to |x|.  Per off-diagonal slot the solve reads 8 B (FP32 value + column) instead
+// of 12 B, and performs no FP64 operation in the SpMV.
+namespace vebi {
+
+struct MxArgs {
+  double *x, *r, *rb, *v, *p, *s, *t, *rinvM, *part, *P;
+  float2 *pi, *si;                     // p_inv, s_inv as (hi, lo)
+  const double *B, *rs;                // right-hand side, FP64 row sums
+  const float* val32;
+  const int *col, *cnt;
+  Scal* sc;
+  long long stride;
+  int n, itermax;
+  double tol;
+};
+
+__device__ __forceinline__ float2 split2(double v) {
+  float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
+__device__ __forceinline__ double join2(float2 q) { return (double)q.x + (double)q.y; }
+
+__device__ __forceinline__ double spmv_diff32(const MxArgs& a, const float2* xv, int i) {
+  const int cnt = __ldg(a.cnt + i);
+  const float* vp = a.val32 + i;
+  const int* cp = a.col + i;
+  const long long st = a.stride;
+  const float2 xi = __ldca(xv + i);
+  float b0 = 0.0f, b1 = 0.0f, b2 = 0.0f, b3 = 0.0f;
+  int k = 0;
+  for (; k + 3 < cnt; k += 4) {
+    const int c0 = __ldg(cp), c1 = __ldg(cp + st), c2 = __ldg(cp + 2 * st), c3 = __ldg(cp + 3 * st);
+    const float v0 = __ldg(vp), v1 = __ldg(vp + st), v2 = __ldg(vp + 2 * st), v3 = __ldg(vp + 3 * st);
+    const float2 x0 = __ldca(xv + c0), x1 = __ldca(xv + c1), x2 = __ldca(xv + c2), x3 = __ldca(xv + c3);
+    b0 = fmaf(v0, (x0.x - xi.x) + (x0.y - xi.y), b0);
+    b1 = fmaf(v1, (x1.x - xi.x) + (x1.y - xi.y), b1);
+    b2 = fmaf(v2, (x2.x - xi.x) + (x2.y - xi.y), b2);
+    b3 = fmaf(v3, (x3.x - xi.x) + (x3.y - xi.y), b3);
+    cp += 4 * st;
+    vp += 4 * st;
+  }
+  for (; k < cnt; ++k) {
+    const float2 x0 = __ldca(xv + __ldg(cp));
+    b0 = fmaf(__ldg(vp), (x0.x - xi.x) + (x0.y - xi.y), b0);
+    cp += st;
+    vp += st;
+  }
+  return fma(__ldg(a.rs + i), join2(xi), (double)((b0 + b1) + (b2 + b3)));
+}
+
+template <bool NONULL>
+__global__ void __launch_bounds__(TPB, 5) k_bicgstab_mixed(MxArgs a) {
+  __shared__ double sh[64];
+  __shared__ double shv[4];
+  const int n = a.n;
+  const int nb = gridDim.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int stride = gridDim.x * blockDim.x;
+  Scal* s = a.sc;
+  double* part = a.part;
+  const double rinv1 = 1.0 / (1.0 + 1.0e-15);
+  const double small = NONULL ? 1.0e-6 : 4.0;
+  double red[2];
+  double acc = 0.0;
+  for (int i = tid; i < n; i += stride) {
+    double bi = a.B[i];
+    a.x[i] = 0.0;
+    a.r[i] = bi;
+    a.rb[i] = bi;
+    a.v[i] = 0.0;
+    a.p[i] = 0.0;
+    acc = fma(bi, bi, acc);
+  }
+  write_partials(acc, 0.0, 1, part + 10 * (size_t)nb, sh);
+  if (!grid_sync(s)) return;
+  reduce_partials(part + 10 * (size_t)nb, nb, 1, red, shv);
+  double rho = red[0], rho0 = 1.0, alpha = 1.0, omega = 1.0;
+  double n2r0 = 1.0, n2s0 = 1.0, resid = 0.0;
+  int iter = 1, warn = 0;
+  bool done = false;
+  while (iter <= a.itermax) {
+    if (rho == 0.0) { warn |= VEBI_WARN_BICGSTAB_BREAKDOWN; done = true; break; }
+    const double beta = rho / (rho0 + 1.0e-15) * alpha / (omega + 1.0e-15);
+    acc = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      double pi = (iter == 1) ? a.r[i] : fma(beta, fma(-omega, a.v[i], a.p[i]), a.r[i]);
+      a.p[i] = pi;
+      acc += pi;
+    }
+    double mean = 0.0;
+    if (NONULL) {
+      write_partials(acc, 0.0, 1, part, sh);
+      if (!grid_sync(s)) return;
+      reduce_partials(part, nb, 1, red, shv);
+      mean = red[0] / (double)n;
+    }
+    for (int i = tid; i < n; i += stride) {
+      double pi = a.p[i];
+      if (NONULL) { pi = pi - mean; a.p[i] = pi; }
+      a.pi[i] = split2(NONULL ? pi * rinv1 : pi * a.rinvM[i]);
+    }
+    if (!grid_sync(s)) return;
+    acc = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      double vi = spmv_diff32(a, a.pi, i);
+      a.v[i] = vi;
+      acc = fma(a.rb[i], vi, acc);
+    }
+    write_partials(acc, 0.0, 1, part + 2 * (size_t)nb, sh);
+    if (!grid_sync(s)) return;
+    reduce_partials(part + 2 * (size_t)nb, nb, 1, red, shv);
+    alpha = rho / (red[0] + 1.0e-15);
+    double a2 = 0.0;
+    acc = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      double si = fma(-alpha, a.v[i], a.r[i]);
+      a.s[i] = si;
+      acc = fma(si, si, acc);
+      a2 += si;
+    }
+    write_partials(acc, a2, 2, part + 4 * (size_t)nb, sh);
+    if (!grid_sync(s)) return;
+    reduce_partials(part + 4 * (size_t)nb, nb, 2, red, shv);
+    const double n2s = red[0];
+    const double mean_s = red[1] / (double)n;
+    if (iter == 1) n2s0 = (n2s <= small) ? 1.0 : n2s;
+    if (n2s <= a.tol * a.tol * n2s0) {
+      for (int i = tid; i < n; i += stride) a.x[i] = fma(alpha, join2(a.pi[i]), a.x[i]);
+      resid = sqrt(n2s / n2s0);
+      done = true;
+      break;
+    }
+    for (int i = tid; i < n; i += stride) {
+      double si = a.s[i];
+      if (NONULL) { si = si - mean_s; a.s[i] = si; }
+      a.si[i] = split2(NONULL ? si * rinv1 : si * a.rinvM[i]);
+    }
+    if (!grid_sync(s)) return;
+    acc = 0.0;
+    a2 = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      double ti = spmv_diff32(a, a.si, i);
+      a.t[i] = ti;
+      acc = fma(ti, a.s[i], acc);
+      a2 = fma(ti, ti, a2);
+    }
+    write_partials(acc, a2, 2, part + 6 * (size_t)nb, sh);
+    if (!grid_sync(s)) return;
+    reduce_partials(part + 6 * (size_t)nb, nb, 2, red, shv);
+    omega = red[0] / (red[1] + 1.0e-15);
+    acc = 0.0;
+    a2 = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      a.x[i] = fma(omega, join2(a.si[i]), fma(alpha, join2(a.pi[i]), a.x[i]));
+      double ri = fma(-omega, a.t[i], a.s[i]);
+      a.r[i] = ri;
+      acc = fma(ri, ri, acc);
+      a2 = fma(a.rb[i], ri, a2);
+    }
+    write_partials(acc, a2, 2, part + 8 * (size_t)nb, sh);
+    if (!grid_sync(s)) return;
+    reduce_partials(part + 8 * (size_t)nb, nb, 2, red, shv);
+    const double n2r = red[0];
+    if (iter == 1) n2r0 = (n2r <= small) ? 1.0 : n2r;
+    resid = sqrt(n2r / n2r0);
+    if (n2r <= a.tol * a.tol * n2r0) { done = true; break; }
+    iter = iter + 1;
+    rho0 = rho;
+    rho = red[1];
+  }
+  if (!done) warn |= VEBI_WARN_MAXITER;
+  for (int i = tid; i < n; i += stride) a.P[i] = a.x[i];
+  if (tid == 0) {
+    s->ls_iters = iter;
+    s->ls_iters_total += iter;
+    s->ls_residual = resid;
+    atomicOr(&s->warnings, warn);
+  }
+}
+
+// FP32 copy of the off-diagonal values and the FP64 row sums; for the Jacobi solver 1/(M+1e-15)
+__global__ void k_matrix_mixed(Consts c, Dev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.npfb) return;
+  double rs = d.ppe_diag[i];
+  const int cnt = d.ij_count[i];
+  for (int k = 0; k < cnt; ++k) {
+    double v = d.ppe_val[ELL(k, i)];
+    rs += v;
+    d.ppe_val32[ELL(k, i)] = (float)v;
+  }
+  d.rowsum[i] = rs;
+  if (c.open_domain == 1) d.bM[i] = 1.0 / (d.ppe_diag[i] + 1.0e-15);
+}
+
+int ppe_mixed_blocks(int nsm) {
+  int per = 0, per2 = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_bicgstab_mixed<true>, TPB, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, k_bicgstab_mixed<false>, TPB, 0);
+  per = per < per2 ? per : per2;
+  if (per < 1) per = 1;
+  return per * nsm;
+}
+
+void launch_ppe_mixed_solve(Ctx& x) {
+  const Consts& c = x.c;
+  VEBI_LAUNCH(x, k_matrix_mixed, grid_for(c.npfb), TPB, c, x.d);
+  int nblk = x.coop_blocks_mixed;
+  long long need = (c.npfb + TPB - 1) / TPB;
+  if (need < nblk) nblk = (int)(need < 1 ? 1 : need);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nblk);
+  cfg.blockDim = dim3(TPB);
+  cfg.stream = x.st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const Dev& d = x.d;
+  MxArgs a{d.bx, d.br, d.brb, d.bv, d.bp, d.bs, d.bt, d.bM, d.partials, d.p, d.pi2, d.si2, d.ppe_B, d.rowsum,
+           d.ppe_val32, d.ppe_col, d.ij_count, d.s, (long long)c.npfb, c.npfb, c.itermax, c.tol};
+  if (c.open_domain == 0) cudaLaunchKernelEx(&cfg, k_bicgstab_mixed<true>, a);
+  else cudaLaunchKernelEx(&cfg, k_bicgstab_mixed<false>, a);
   x.launches++;
 }
 

@@ -361,8 +361,10 @@ __device__ __forceinline__ void pgrad_one(const Consts& c, const Dev& d, int i, 
       ux = d.u0x[i] + dt * c.bf[0];
       uy = d.u0y[i] + dt * c.bf[1];
     }
-    x = d.r0x[i] + 0.5 * (ux + d.u0x[i]) * dt + d.ushx[i] * dt;
-    y = d.r0y[i] + 0.5 * (uy + d.u0y[i]) * dt + d.ushy[i] * dt;
+    if (!c.correct_velocity) {  // else k_advect_final moves the particles after the correction
+      x = d.r0x[i] + 0.5 * (ux + d.u0x[i]) * dt + d.ushx[i] * dt;
+      y = d.r0y[i] + 0.5 * (uy + d.u0y[i]) * dt + d.ushy[i] * dt;
+    }
   }
   d.ux[i] = ux;
   d.uy[i] = uy;
@@ -386,9 +388,54 @@ __global__ void k_pgrad_final(Consts c, Dev d) {
 }
 
 
+// correct_velocity (correct_velocity.F90:13-70), behind a switch: the reference has the call
+// commented out (div_free.F90:105).  Particles closer than dx to a wall (or wall-wall corner)
+// mirror lose the velocity component towards it.  A circle mirror (vrelation = 999+ib) is not
+// treated as a wall: the reference indexes b_type out of range there.
+__global__ void k_correct_velocity(Consts c, Dev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < c.nbS || i >= c.npfb) return;
+  const double xi = d.rx[i], yi = d.ry[i];
+  double r_min2 = c.dx * c.dx;
+  int close = -1;
+  const int cnt = d.ij_count[i];
+  for (int k = 0; k < cnt; ++k) {
+    int j = d.ij_link[ELL(k, i)];
+    if (j < c.npfb) continue;
+    double a = xi - d.rx[j], b = yi - d.ry[j];
+    double d2 = a * a + b * b;
+    if (!(d2 < r_min2)) continue;
+    int vr = d.vrel[j];
+    if (vr > 0 && vr < 999 && c.b_type[vr - 1] == 1) { r_min2 = d2; close = j; }
+    if (vr == -1 || vr < -2) { r_min2 = d2; close = j; }
+  }
+  if (close < 0) return;
+  double n1 = xi - d.rx[close], n2 = yi - d.ry[close];
+  double t = sqrt(n1 * n1 + n2 * n2);
+  n1 = n1 / t;
+  n2 = n2 / t;
+  double u1 = d.ux[i] - d.ux2[close], u2 = d.uy[i] - d.uy2[close];
+  double un = u1 * n1 + u2 * n2;
+  if (un <= 0.0) {
+    d.ux[i] = d.ux[i] - un * n1;
+    d.uy[i] = d.uy[i] - un * n2;
+  }
+}
+
+// final advection after correct_velocity (div_free.F90:111-117)
+__global__ void k_advect_final(Consts c, Dev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < c.nbS || i >= c.npfb) return;
+  const double dt = d.s->dt;
+  d.rx[i] = d.r0x[i] + 0.5 * (d.ux[i] + d.u0x[i]) * dt + d.ushx[i] * dt;
+  d.ry[i] = d.r0y[i] + 0.5 * (d.uy[i] + d.u0y[i]) * dt + d.ushy[i] * dt;
+}
+
 // secondary_properties: vorticity from final fluid u and mirror u* (div_free.F90:160-183)
+template <typename W>
 __global__ void k_secondary(Consts c, Dev d, const double* __restrict__ uxn, const double* __restrict__ uyn,
-                            const double* __restrict__ uxm, const double* __restrict__ uym) {
+                            const double* __restrict__ uxm, const double* __restrict__ uym,
+                            const W* __restrict__ wgx, const W* __restrict__ wgy) {
   __shared__ double sh[TPB / 32 + 1];
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   double e = 0.0;
@@ -399,7 +446,7 @@ __global__ void k_secondary(Consts c, Dev d, const double* __restrict__ uxn, con
     for (int k = 0; k < cnt; ++k) {
       int j = d.ij_link[ELL(k, i)];
       double uj = j < c.npfb ? uxn[j] : uxm[j], vj = j < c.npfb ? uyn[j] : uym[j];
-      double tmp = (vi - vj) * d.wGx[ELL(k, i)] - (ui - uj) * d.wGy[ELL(k, i)];
+      double tmp = (vi - vj) * (double)wgx[ELL(k, i)] - (ui - uj) * (double)wgy[ELL(k, i)];
       vt = vt - tmp;
     }
     d.vort[i] = vt;
@@ -417,10 +464,19 @@ __global__ void k_secondary_final(Consts c, Dev d, int nblk) {
   if (threadIdx.x == 0) d.s->rms_u = sqrt(s / (double)c.npfb);
 }
 
+void launch_prep_weights32(Ctx& x);
+void launch_shift32(Ctx& x);
+void launch_gradients32(Ctx& x);
+void launch_predictor32(Ctx& x);
+void launch_pgrad_final32(Ctx& x);
+
 void launch_weights_surface_shift(Ctx& x) {
   const Consts& c = x.c;
   int g = grid_for(c.npfb);
-  VEBI_LAUNCH(x, k_weights, g, TPB, c, x.d);
+  const bool mixed = x.precision == VEBI_PREC_MIXED;
+  if (mixed) launch_prep_weights32(x);
+  // FP64 weights: the FP64 step, and the free-surface operators of an open domain
+  if (!mixed || c.open_domain == 1) VEBI_LAUNCH(x, k_weights, g, TPB, c, x.d);
   if (c.open_domain == 1) {
     VEBI_LAUNCH(x, k_part_dist_vars, g, TPB, c, x.d);
     VEBI_LAUNCH(x, k_nsurf_mirrors, x.gs_blocks, TPB, c, x.d);
@@ -430,7 +486,8 @@ void launch_weights_surface_shift(Ctx& x) {
     cudaMemsetAsync(x.d.n_surf, 0, sizeof(int) * (size_t)c.cap, x.st);
   }
   stage_mark(x, 5);
-  VEBI_LAUNCH(x, k_shift, g, TPB, c, x.d);
+  if (mixed && c.open_domain == 0) launch_shift32(x);
+  else VEBI_LAUNCH(x, k_shift, g, TPB, c, x.d);
 }
 
 void launch_grad_mirrors(Ctx& x);
@@ -441,8 +498,10 @@ void launch_mirror_pressure(Ctx& x);
 void launch_predictor(Ctx& x) {
   const Consts& c = x.c;
   int g = grid_for(c.npfb);
+  const bool mixed = x.precision == VEBI_PREC_MIXED;
   stage_mark(x, 6);
-  VEBI_LAUNCH(x, k_gradients, g, TPB, c, x.d);
+  if (mixed) launch_gradients32(x);
+  else VEBI_LAUNCH(x, k_gradients, g, TPB, c, x.d);
   launch_grad_mirrors(x);
   stage_mark(x, 7);
   if (c.const_mod != 1) {
@@ -450,7 +509,8 @@ void launch_predictor(Ctx& x) {
     launch_mirror_stress(x);
   }
   stage_mark(x, 8);
-  VEBI_LAUNCH(x, k_predictor, g, TPB, c, x.d);
+  if (mixed) launch_predictor32(x);
+  else VEBI_LAUNCH(x, k_predictor, g, TPB, c, x.d);
   launch_mirror_velocities(x);
   // theta* replaces theta for walls and fluid; u* stays in ux2/uy2 for the PPE and the update
   cudaMemcpyAsync(x.d.th, x.d.th2, sizeof(double) * (size_t)c.npfb, cudaMemcpyDeviceToDevice, x.st);
@@ -464,10 +524,17 @@ void launch_final(Ctx& x, int secondary) {
   // keep r* (fluid and mirrors) readable after the step: the update below overwrites r
   cudaMemcpyAsync(x.d.rx2, x.d.rx, sizeof(double) * (size_t)c.cap, cudaMemcpyDeviceToDevice, x.st);
   cudaMemcpyAsync(x.d.ry2, x.d.ry, sizeof(double) * (size_t)c.cap, cudaMemcpyDeviceToDevice, x.st);
-  VEBI_LAUNCH(x, k_pgrad_final, g, TPB, c, x.d);
+  const bool mixed = x.precision == VEBI_PREC_MIXED;
+  if (mixed) launch_pgrad_final32(x);
+  else VEBI_LAUNCH(x, k_pgrad_final, g, TPB, c, x.d);
+  if (c.correct_velocity) {
+    VEBI_LAUNCH(x, k_correct_velocity, g, TPB, c, x.d);
+    VEBI_LAUNCH(x, k_advect_final, g, TPB, c, x.d);
+  }
   if (secondary) {
     stage_mark(x, 13);
-    VEBI_LAUNCH(x, k_secondary, g, TPB, c, x.d, x.d.ux, x.d.uy, x.d.ux2, x.d.uy2);
+    if (mixed) VEBI_LAUNCH(x, k_secondary<float>, g, TPB, c, x.d, x.d.ux, x.d.uy, x.d.ux2, x.d.uy2, x.d.wGx32, x.d.wGy32);
+    else VEBI_LAUNCH(x, k_secondary<double>, g, TPB, c, x.d, x.d.ux, x.d.uy, x.d.ux2, x.d.uy2, x.d.wGx, x.d.wGy);
     VEBI_LAUNCH(x, k_secondary_final, 1, TPB, c, x.d, g);
   }
 }
