@@ -135,6 +135,8 @@ def make_case(args):
         return cases.poiseuille(1000, seed=args.seed)
     if args.case == "cavity_1m":
         return cases.cavity(1024, seed=args.seed)
+    if args.case == "poiseuille_40":
+        return cases.poiseuille(40, seed=args.seed)
     raise SystemExit(f"unknown case {args.case}")
 
 
@@ -183,6 +185,7 @@ def run_gb300(args, dist: Dist):
     case = make_case(args)
     if args.itermax:
         case.itermax = args.itermax
+    case.ppe_warm_start = 1 if args.warm_start else 0
     prec = abi.PREC_MIXED if args.precision == "mixed" else abi.PREC_FP64
     sol = StepSolver(case, precision=prec, timing=True)
     n_fluid = case.n_fluid
@@ -363,6 +366,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision comparison run")
+    ap.add_argument("--warm-start", action="store_true",
+                    help="opt-in: PPE starts from the previous step's pressure (changes results)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

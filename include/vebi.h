@@ -103,7 +103,9 @@ typedef struct vebi_params {
   int32_t precision;                   /* VEBI_PREC_*                                            */
   int32_t correct_velocity;            /* 1: run correct_velocity after the update; the reference
                                           has the call commented out (div_free.F90:105)          */
-  int32_t reserved[6];
+  int32_t ppe_warm_start;              /* 1: start BiCGSTAB from the previous step's P instead of
+                                          x0 = 0 (ppe...:145); changes results, off by default   */
+  int32_t reserved[5];
 } vebi_params;
 
 /* Per-step scalars the Fortran driver and `output` read after div_free

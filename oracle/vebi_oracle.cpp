@@ -1291,6 +1291,8 @@ struct Oracle {
       }
     }
     std::vector<double> x(npfb, 0.0);
+    if (P.ppe_warm_start)  // opt-in: start from the previous step's P (the reference uses 0)
+      for (int i = 0; i < npfb; ++i) x[i] = p[i];
     mark(10);
     double t0 = wtime();
     bicgstab(x, ppe_B, P.i_open_domain == 0);

@@ -109,3 +109,17 @@ def test_multistep_poiseuille_fields(libs):
         scale = np.abs(b).max()
         assert np.abs(a - b).max() <= 10.0 * spread + 1e-12 * scale, name
     assert abs(sg["dt"] - so["dt"]) <= 1e-9 * so["dt"]
+
+
+def test_warm_start_multistep(libs):
+    """Opt-in PPE warm start (x0 = previous P): GPU and oracle agree over 5 steps."""
+    StepSolver, OracleSolver = libs
+    case = _with(cases.poiseuille(40, seed=8), ppe_warm_start=1)
+    gpu, ref = StepSolver(case), OracleSolver(case)
+    for _ in range(5):
+        sg, so = gpu.step(), ref.step()
+    n = case.npfb
+    us = max(np.abs(ref.get("ux")[:n]).max(), np.abs(ref.get("uy")[:n]).max())
+    for nm in ("ux", "uy"):
+        assert np.abs(gpu.get(nm)[:n] - ref.get(nm)[:n]).max() < 1e-6 * us, nm
+    assert sg["LS_residual"] <= 1e-8 and so["LS_residual"] <= 1e-8

@@ -57,7 +57,7 @@ class VebiParams(C.Structure):
         ("npfb", C.c_int32), ("nbS", C.c_int32),
         ("const_mod", C.c_int32), ("itermax", C.c_int32), ("nplink", C.c_int32),
         ("nmirror_cap", C.c_int32), ("precision", C.c_int32), ("correct_velocity", C.c_int32),
-        ("reserved", C.c_int32 * 6),
+        ("ppe_warm_start", C.c_int32), ("reserved", C.c_int32 * 5),
     ]
 
 

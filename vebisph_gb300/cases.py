@@ -68,6 +68,7 @@ class Case:
     nplink: int = 75
     nmirror_cap: int = 0
     correct_velocity: int = 0
+    ppe_warm_start: int = 0
 
     def __post_init__(self):
         n = self.npfb
@@ -135,6 +136,7 @@ class Case:
         p.nmirror_cap = self.nmirror_cap
         p.precision = precision
         p.correct_velocity = self.correct_velocity
+        p.ppe_warm_start = self.ppe_warm_start
         return p
 
     def fortran_planes(self, ld: int | None = None) -> dict:

@@ -100,6 +100,7 @@ static int build_consts(Ctx& x) {
   c.shift_coeff = P.i_shift_coeff;
   c.const_mod = P.const_mod == 1 ? 1 : 2;
   c.correct_velocity = P.correct_velocity ? 1 : 0;
+  c.warm_start = P.ppe_warm_start ? 1 : 0;
   c.npfb = P.npfb;
   c.nbS = P.nbS;
   for (int i = 0; i < nb; ++i) {

@@ -42,6 +42,7 @@ struct Consts {
   int npfb, nbS, cap, mcap, nplink;
   int open_domain, shift_coeff, const_mod, itermax;
   int correct_velocity;                             // run correct_velocity (off in the reference)
+  int warm_start;                                   // PPE starts from the previous P (opt-in)
 };
 
 // Scalars that change during a step; they live in device memory so no step needs a host sync.

@@ -182,6 +182,7 @@ struct BiArgs {
   long long stride;
   int n, itermax;
   double tol;
+  int warm;
 };
 
 // y_i = A_ii x_i + sum_k A_ik x_col(ik)  (sparse_atime, linear_solver.F90:254-273).  Four
@@ -232,9 +233,18 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
   const double small = NONULL ? 1.0e-6 : 4.0;  // open solver: the integer expression 10-6
   double red[2];
   double acc = 0.0;
+  if (a.warm) {  // x0 = P of the previous step: r0 = B - A x0 (the SpMV reads x through pinv)
+    for (int i = tid; i < n; i += stride) {
+      double xi = a.P[i];
+      a.x[i] = xi;
+      a.pinv[i] = xi;
+    }
+    if (!grid_sync(s)) return;
+  }
   for (int i = tid; i < n; i += stride) {
     double bi = a.B[i];
-    a.x[i] = 0.0;
+    if (a.warm) bi = bi - spmv_row(a, a.pinv, i);
+    else a.x[i] = 0.0;
     a.r[i] = bi;
     a.rb[i] = bi;
     a.v[i] = 0.0;
@@ -406,7 +416,8 @@ void launch_ppe(Ctx& x) {
   cfg.numAttrs = 1;
   const Dev& d = x.d;
   BiArgs a{d.bx, d.br, d.brb, d.bv, d.bp, d.bpi, d.bs, d.bsi, d.bt, d.bM, d.partials, d.p,
-           d.ppe_B, d.ppe_diag, d.ppe_val, d.ppe_col, d.ij_count, d.s, (long long)c.npfb, c.npfb, c.itermax, c.tol};
+           d.ppe_B, d.ppe_diag, d.ppe_val, d.ppe_col, d.ij_count, d.s, (long long)c.npfb, c.npfb, c.itermax, c.tol,
+           c.warm_start};
   if (c.open_domain == 0) cudaLaunchKernelEx(&cfg, k_bicgstab<true>, a);
   else cudaLaunchKernelEx(&cfg, k_bicgstab<false>, a);
   x.launches++;
@@ -441,6 +452,7 @@ struct MxArgs {
   long long stride;
   int n, itermax;
   double tol;
+  int warm;
 };
 
 __device__ __forceinline__ float2 split2(double v) {
@@ -491,9 +503,18 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab_mixed(MxArgs a) {
   const double small = NONULL ? 1.0e-6 : 4.0;
   double red[2];
   double acc = 0.0;
+  if (a.warm) {  // x0 = P of the previous step
+    for (int i = tid; i < n; i += stride) {
+      double xi = a.P[i];
+      a.x[i] = xi;
+      a.pi[i] = split2(xi);
+    }
+    if (!grid_sync(s)) return;
+  }
   for (int i = tid; i < n; i += stride) {
     double bi = a.B[i];
-    a.x[i] = 0.0;
+    if (a.warm) bi = bi - spmv_diff32(a, a.pi, i);
+    else a.x[i] = 0.0;
     a.r[i] = bi;
     a.rb[i] = bi;
     a.v[i] = 0.0;
@@ -648,7 +669,7 @@ void launch_ppe_mixed_solve(Ctx& x) {
   cfg.numAttrs = 1;
   const Dev& d = x.d;
   MxArgs a{d.bx, d.br, d.brb, d.bv, d.bp, d.bs, d.bt, d.bM, d.partials, d.p, d.pi2, d.si2, d.ppe_B, d.rowsum,
-           d.ppe_val32, d.ppe_col, d.ij_count, d.s, (long long)c.npfb, c.npfb, c.itermax, c.tol};
+           d.ppe_val32, d.ppe_col, d.ij_count, d.s, (long long)c.npfb, c.npfb, c.itermax, c.tol, c.warm_start};
   if (c.open_domain == 0) cudaLaunchKernelEx(&cfg, k_bicgstab_mixed<true>, a);
   else cudaLaunchKernelEx(&cfg, k_bicgstab_mixed<false>, a);
   x.launches++;
