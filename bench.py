@@ -289,6 +289,106 @@ def run_gb300(args, dist: Dist):
     return res
 
 
+def run_batch(args, dist: Dist):
+    """The batched parameter sweep: args.batch independent Poiseuille/cylinder instances with
+    log-uniform fluid counts in 4k-256k, Wi ~ U[0.1, 4], beta ~ U[0.1, 0.9] (seeded), mixed
+    precision, advanced together by vebi_batch_step (one CUDA-graph launch per step), against the
+    same instances run one by one with the plain FP64 step.  Each instance's velocity error is
+    max |u_mixed - u_fp64| / max |u_fp64| after the same steps from the same initial state."""
+    from vebisph_gb300 import abi, cases
+    from vebisph_gb300.solver import BatchSolver, StepSolver, VebiError
+
+    cl = cases.batch_sweep(args.batch, seed=args.seed)
+    n_fluid = sum(c.n_fluid for c in cl)
+    t0 = time.perf_counter()
+    bprec = abi.PREC_MIXED if args.batch_precision == "mixed" else abi.PREC_FP64
+    b = BatchSolver(cl, precision=bprec)
+    t_create = time.perf_counter() - t0
+    tune = b.autotune(candidates=tuple(int(v) for v in args.tune.split(",")))
+    done = 2 * len(tune["ms_per_candidate"])
+    for _ in range(args.warmup):
+        b.step(1)
+    dist.barrier()
+    with ClockSampler(dist.local) as clk:
+        ms, stats = b.step(args.steps)
+    dist.barrier()
+    done += args.warmup + args.steps
+    t_max = dist.max(ms)
+    fields = [{k: inst.get(k)[: c.npfb].copy() for k in ("ux", "uy", "p")} for inst, c in zip(b.instances, cl)]
+    iters = [st["LS_iters_total"] / args.steps for st in stats]
+    failed = {i: st["error"] for i, st in enumerate(stats) if st["error"]}
+    b.close()
+    # only instances that stepped without failure count as work
+    n_live = sum(c.n_fluid for i, c in enumerate(cl) if i not in failed)
+    value = dist.sum(float(n_live * args.steps)) / (t_max * 1e-3)
+    # the same instances one by one, plain FP64, timed over the same K steps (device events)
+    serial_ms, serial_units, du, dp, per = 0.0, 0, [], [], []
+    for i, (c, fm) in enumerate(zip(cl, fields)):
+        s1 = StepSolver(c, precision=abi.PREC_FP64)
+        rec = {"i": i, "case": c.name, "n_fluid": c.n_fluid, "El": c.El, "beta": c.beta,
+               "batch_error": failed.get(i, 0), "LS_iters_batch": iters[i]}
+        try:
+            for _ in range(done - args.steps):
+                s1.step()
+            m1, st1 = s1.run_steps(args.steps)
+            serial_ms += m1
+            serial_units += c.n_fluid * args.steps
+            rec["LS_iters_fp64"] = st1["LS_iters_total"] / args.steps
+            ux, uy, pp = (s1.get(k)[: c.npfb] for k in ("ux", "uy", "p"))
+            if not (np.isfinite(ux).all() and np.isfinite(uy).all() and np.isfinite(pp).all()):
+                rec["fp64_error"] = "non-finite"
+            elif i not in failed:
+                us = max(np.abs(ux).max(), np.abs(uy).max(), 1e-300)
+                rec["du"] = float(max(np.abs(fm["ux"] - ux).max(), np.abs(fm["uy"] - uy).max()) / us)
+                rec["dp"] = float(np.abs(fm["p"] - pp).max() / max(np.abs(pp).max(), 1e-300))
+                if not np.isfinite(rec["du"]):
+                    rec["du"] = float("inf")
+                du.append(rec["du"])
+                dp.append(rec["dp"])
+        except VebiError as e:
+            rec["fp64_error"] = e.status
+        s1.close()
+        per.append(rec)
+    serial_value = serial_units / (serial_ms * 1e-3)
+    du, dp = np.array(du), np.array(dp)
+    counts = np.array([c.n_fluid for c in cl])
+    try:
+        (ROOT / "gpurun_out").mkdir(exist_ok=True)
+        (ROOT / "gpurun_out" / f"batch{args.batch}_instances.json").write_text(json.dumps(per))
+    except OSError:
+        pass
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if bprec == abi.PREC_MIXED else "f64",
+        "data": "synthetic: seeded jittered lattices, walls/circle by the reference's make_boundary_particles rules",
+        "config": {"workload": f"batch{args.batch}: {args.batch} independent instances (even: Poiseuille channel, "
+                               f"odd: confined cylinder), fluid counts log-uniform 4k-256k, Wi~U[0.1,4], "
+                               f"beta~U[0.1,0.9], seed {args.seed}, {args.batch_precision}",
+                   "instances": args.batch, "n_fluid_total": n_fluid,
+                   "n_fluid_min": int(counts.min()), "n_fluid_max": int(counts.max()),
+                   "parallelism": f"batch (one CUDA graph per step, {args.batch} branches) x{dist.world} replicas",
+                   "l2": f"inputs larger than L2 (all instances' arrays resident: {n_fluid} particles)",
+                   "autotune": tune, "create_s": round(t_create, 2)},
+        "gpu_launches": int(sum(st["gpu_launches"] for st in stats)),
+        "LS_iters_per_step": {"mean": float(np.mean(iters)), "max": float(np.max(iters))},
+        "failed_instances": {"batch": len(failed), "serial_fp64": sum(1 for r in per if "fp64_error" in r),
+                             "both": sum(1 for r in per if "fp64_error" in r and r["batch_error"]),
+                             "statuses": sorted(set(failed.values()))},
+        "serial_fp64": {"value": serial_value, "unit": UNIT, "ms_per_step": serial_ms / args.steps,
+                        "speedup_of_batch": value / serial_value, "counted": "instances that did not fail",
+                        "path": "one StepSolver per instance, FP64, graph-replayed steps, summed device time"},
+        "batch_vs_serial_fp64": ({
+            "compared": int(du.size), "note": "instances where neither run failed; u = max|du|/max|u_fp64|",
+            "u_rel_median": float(np.median(du)), "u_rel_p90": float(np.percentile(du, 90)),
+            "u_within_1e-4": int((du <= 1e-4).sum()), "u_within_1e-3": int((du <= 1e-3).sum()),
+            "u_within_1e-2": int((du <= 1e-2).sum()), "p_rel_median": float(np.median(dp))}
+            if du.size else None),
+        "roofline": None,
+        "clocks": clk.summary(),
+    }
+
+
 def mixed_summary(f64: dict, mx: dict) -> dict:
     """Speed of the mixed step and its difference from the FP64 step after the same steps from
     the same initial state: velocity and pressure (max abs difference / max abs FP64 value),
@@ -366,11 +466,18 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision comparison run")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="run the batched parameter sweep of this many instances instead")
+    ap.add_argument("--batch-precision", choices=["fp64", "mixed"], default="mixed")
+    ap.add_argument("--tune", default="1,2,4", help="solver rows-per-thread candidates of the batch autotuner")
     ap.add_argument("--warm-start", action="store_true",
                     help="opt-in: PPE starts from the previous step's pressure (changes results)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.batch:
+        # independent instances run as concurrent graph branches: more hardware queues
+        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     dist = Dist()
     if args.impl == "gb300":
         import __graft_entry__ as g
@@ -382,8 +489,11 @@ def main():
             vis = os.environ.get("CUDA_VISIBLE_DEVICES")
             ids = vis.split(",") if vis else [str(i) for i in range(dist.world)]
             os.environ["CUDA_VISIBLE_DEVICES"] = ids[dist.local % len(ids)]
-        res = run_gb300(args, dist)
-        if args.precision == "fp64" and not args.no_mixed:
+        if args.batch:
+            res = run_batch(args, dist)
+        else:
+            res = run_gb300(args, dist)
+        if args.precision == "fp64" and not args.no_mixed and not args.batch:
             # the mixed-precision step on the same workload: its speed and its distance from FP64
             margs = argparse.Namespace(**vars(args))
             margs.precision = "mixed"

@@ -152,7 +152,9 @@ int vebi_step(vebi_ctx* ctx, double x_mint, double y_mint, double x_maxt, double
 
 /* Run nsteps steps back to back on the context's stream (no host copies) and return
  * the device time between the first launch and the last completion in *ms.  With timing
- * on, last->stage_ms holds each stage's device time summed over the nsteps steps. */
+ * on, last->stage_ms holds each stage's device time summed over the nsteps steps.
+ * A failure in any of the steps is returned (the first failing status is kept on the device
+ * until the next vebi_upload_state; the steps after it skip the PPE solve). */
 int vebi_run_steps(vebi_ctx* ctx, double x_mint, double y_mint, double x_maxt, double y_maxt,
                    int32_t nsteps, double* ms, vebi_step_stats* last);
 
@@ -199,6 +201,29 @@ int vebi_ppe_solve_noalloc(const int32_t* ij_count, const int32_t* ppe_col, cons
                            const double* ppe_diag, const double* rhs, double* x, int32_t n,
                            int64_t ell_stride, int32_t closed_domain, double tol, int32_t itermax,
                            void* stream, int32_t* iters_out, double* residual_out);
+
+/* ---- Batches of independent simulations ----------------------------------------------
+ * No counterpart in the reference, which runs one simulation per process.  A batch owns n
+ * contexts (one per simulation, each with its own device arrays); uneven particle counts and
+ * parameters are allowed.  vebi_batch_step advances every instance by nsteps steps: each step
+ * is one launch of a CUDA graph whose independent branches are the instances' captured steps,
+ * so the instances overlap on the GPU, and the call waits once at the end.  Each instance
+ * keeps its own PPE convergence (iterations and residual in stats[i], an array of n).  An
+ * instance whose step fails reports its status in stats[i].error; the failure is sticky for
+ * that instance until its next upload (its later steps skip the PPE solve) and the other
+ * instances go on: the call returns VEBI_OK unless a CUDA call failed.  Instances are
+ * reached with vebi_batch_get for upload/download/inspection; destroying the batch destroys
+ * them. */
+typedef struct vebi_batch vebi_batch;
+int vebi_batch_create(const vebi_params* params, int32_t n, vebi_batch** out);
+int vebi_batch_get(vebi_batch* b, int32_t i, vebi_ctx** ctx);
+int vebi_batch_step(vebi_batch* b, int32_t nsteps, double* ms, vebi_step_stats* stats);
+int vebi_batch_destroy(vebi_batch* b);
+
+/* Rows of the PPE each solver thread owns (>= 1; default 1): the persistent solver runs on
+ * ceil(npfb / (256 * rows_per_thread)) blocks, at most the co-resident maximum.  Fewer blocks
+ * make a small instance leave room for other instances of a batch.  Re-captures the graph. */
+int vebi_set_solver_grid(vebi_ctx* ctx, int32_t rows_per_thread);
 
 /* Static description of the library build. */
 const char* vebi_version(void);

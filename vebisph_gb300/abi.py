@@ -97,6 +97,7 @@ EXPORTED_SYMBOLS = [
     "vebi_create", "vebi_upload_state", "vebi_step", "vebi_run_steps", "vebi_download_state",
     "vebi_destroy", "vebi_pin_host", "vebi_unpin_host", "vebi_set_timing", "vebi_debug_size",
     "vebi_debug_get", "vebi_version", "vebi_last_error", "vebi_ppe_solve_noalloc",
+    "vebi_batch_create", "vebi_batch_get", "vebi_batch_step", "vebi_batch_destroy", "vebi_set_solver_grid",
 ]
 NOALLOC_MAX_ROWS = 65536
 
@@ -138,6 +139,13 @@ def load_library():
     lib.vebi_ppe_solve_noalloc.argtypes = [vp, vp, vp, vp, vp, vp, C.c_int32, C.c_int64, C.c_int32,
                                            C.c_double, C.c_int32, vp, P(C.c_int32), P(C.c_double)]
     lib.vebi_ppe_solve_noalloc.restype = C.c_int
+    lib.vebi_batch_create.argtypes = [P(VebiParams), C.c_int32, P(vp)]
+    lib.vebi_batch_get.argtypes = [vp, C.c_int32, P(vp)]
+    lib.vebi_batch_step.argtypes = [vp, C.c_int32, P(C.c_double), P(VebiStepStats)]
+    lib.vebi_batch_destroy.argtypes = [vp]
+    lib.vebi_set_solver_grid.argtypes = [vp, C.c_int32]
+    for fn in ("vebi_batch_create", "vebi_batch_get", "vebi_batch_step", "vebi_batch_destroy", "vebi_set_solver_grid"):
+        getattr(lib, fn).restype = C.c_int
     lib.vebi_version.restype = C.c_char_p
     lib.vebi_last_error.restype = C.c_char_p
     for fn in ("vebi_create", "vebi_upload_state", "vebi_step", "vebi_run_steps", "vebi_download_state",

@@ -470,3 +470,21 @@ def by_name(name: str, **kw) -> Case:
         "rb_deck": rayleigh_benard_deck,
     }
     return table[name]()
+
+
+def batch_sweep(n: int = 512, seed: int = 0, lo: float = 4.0e3, hi: float = 2.56e5):
+    """The batched parameter sweep: n instances with fluid counts log-uniform in [lo, hi],
+    Wi ~ U[0.1, 4.0], beta ~ U[0.1, 0.9] (seeded), alternating Poiseuille channel and cylinder
+    geometry."""
+    rng = np.random.default_rng(seed)
+    counts = np.exp(rng.uniform(np.log(lo), np.log(hi), size=n))
+    wis = rng.uniform(0.1, 4.0, size=n)
+    betas = rng.uniform(0.1, 0.9, size=n)
+    out = []
+    for k in range(n):
+        if k % 2 == 0:
+            m = max(8, int(round(math.sqrt(counts[k]))))
+            out.append(poiseuille(m, seed=seed + k, Wi=float(wis[k]), beta=float(betas[k])))
+        else:
+            out.append(cylinder(float(counts[k]), Wi=float(wis[k]), beta=float(betas[k]), seed=seed + k))
+    return out

@@ -307,6 +307,10 @@ int vebi_upload_state(vebi_ctx* h, const double* r, const double* u, const doubl
   if (trace_conf) CUDA_TRY(cudaMemcpyAsync(d.trace_conf, trace_conf, B, cudaMemcpyHostToDevice, x.st));
   if (inbin) CUDA_TRY(cudaMemcpyAsync(d.inbin, inbin, (size_t)n, cudaMemcpyHostToDevice, x.st));
   else CUDA_TRY(cudaMemsetAsync(d.inbin, 0, (size_t)n, x.st));
+  // a new state starts with no recorded failure
+  CUDA_TRY(cudaMemsetAsync(&d.s->first_error, 0, sizeof(int), x.st));
+  CUDA_TRY(cudaMemsetAsync(&d.s->error, 0, sizeof(int), x.st));
+  CUDA_TRY(cudaMemsetAsync(&d.s->n_inbin, 0, sizeof(int), x.st));
   x.have_state = true;
   return VEBI_OK;
 }
@@ -334,7 +338,7 @@ static int finish_step(Ctx& x, vebi_step_stats* stats, bool sync) {
   o.nmirror = s.nmirror;
   o.maxneighbours = s.maxneigh;
   o.n_escapees = s.n_escapees;
-  o.error = s.error;
+  o.error = s.error ? s.error : s.first_error;
   o.warnings = s.warnings | (s.n_escapees ? VEBI_WARN_ESCAPEES : 0);
   o.gpu_launches = x.launches;
   o.refine_iters = s.refine_iters;
@@ -356,6 +360,7 @@ static int finish_step(Ctx& x, vebi_step_stats* stats, bool sync) {
   x.last = o;
   if (stats) *stats = o;
   if (s.error) return fail(s.error, "device-side error in the step");
+  if (s.first_error) return fail(s.first_error, "an earlier step of this state failed");
   if (s.n_inbin == x.c.npfb - x.c.nbS && x.c.npfb > x.c.nbS) return fail(VEBI_ERR_ALL_IN_BIN, "all liquid particles are in the bin");
   return VEBI_OK;
 }
@@ -540,9 +545,206 @@ int vebi_unpin_host(void* ptr) {
   return VEBI_OK;
 }
 
+int vebi_set_solver_grid(vebi_ctx* h, int32_t rows_per_thread) {
+  if (!h || rows_per_thread < 1) return fail(VEBI_ERR_ARG, "bad argument");
+  Ctx& x = h->x;
+  if (x.solver_rows_per_thread == rows_per_thread) return VEBI_OK;
+  cudaStreamSynchronize(x.st);
+  x.solver_rows_per_thread = rows_per_thread;
+  ++x.grid_gen;
+  for (int m = 0; m < 2; ++m) {  // the captured steps hold the old grid
+    if (x.graph[m]) cudaGraphExecDestroy(x.graph[m]);
+    x.graph[m] = nullptr;
+    x.graph_failed[m] = false;
+  }
+  return VEBI_OK;
+}
+
 int vebi_set_timing(vebi_ctx* h, int32_t on) {
   if (!h) return fail(VEBI_ERR_ARG, "null context");
   h->x.timing = on != 0;
+  return VEBI_OK;
+}
+
+// ------------------------------------------------------------------ batches
+// A batch is a set of independent contexts (one per simulation, each with its own sizes,
+// parameters and device arrays).  One batch step is one launch of a CUDA graph whose
+// independent branches are the instances' captured steps, so the instances' kernels overlap
+// on the GPU with no host work between them; each instance's solver converges on its own.
+struct vebi_batch {
+  std::vector<vebi_ctx*> ctx;
+  cudaGraphExec_t graph = nullptr;
+  bool graph_failed = false;
+  std::vector<int> launches;  // kernels in each instance's captured step
+  std::vector<int> gen;  // grid_gen of each instance when the batch graph was captured
+};
+
+static void batch_drop_graph(vebi_batch* b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+  b->graph_failed = false;
+}
+
+// capture every instance's step into a child graph of one batch graph
+static bool batch_graph_ready(vebi_batch* b) {
+  const int n = (int)b->ctx.size();
+  if (b->graph) {
+    bool stale = false;
+    for (int i = 0; i < n; ++i) stale |= b->gen[i] != b->ctx[i]->x.grid_gen;
+    if (!stale) return true;
+    batch_drop_graph(b);
+  }
+  if (b->graph_failed) return false;
+  cudaGraph_t bg = nullptr;
+  if (cudaGraphCreate(&bg, 0) != cudaSuccess) {
+    cudaGetLastError();
+    b->graph_failed = true;
+    return false;
+  }
+  std::vector<int> launches(n, 0);
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < n && e == cudaSuccess; ++i) {
+    Ctx& x = b->ctx[i]->x;
+    const bool timing = x.timing;
+    x.timing = false;
+    x.launches = 0;
+    cudaGraph_t g = nullptr;
+    e = cudaStreamBeginCapture(x.st, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      x.capturing = true;
+      enqueue_step(x, 0);
+      x.capturing = false;
+      e = cudaStreamEndCapture(x.st, &g);
+    }
+    x.timing = timing;
+    cudaGraphNode_t node;
+    if (e == cudaSuccess && g) e = cudaGraphAddChildGraphNode(&node, bg, nullptr, 0, g);
+    if (g) cudaGraphDestroy(g);
+    launches[i] = x.launches;
+  }
+  cudaGraphExec_t ge = nullptr;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, bg, 0);
+  cudaGraphDestroy(bg);
+  if (e != cudaSuccess || !ge) {
+    cudaGetLastError();
+    b->graph_failed = true;
+    return false;
+  }
+  b->graph = ge;
+  b->launches = launches;
+  b->gen.resize(n);
+  for (int i = 0; i < n; ++i) b->gen[i] = b->ctx[i]->x.grid_gen;
+  return true;
+}
+
+int vebi_batch_create(const vebi_params* params, int32_t n, vebi_batch** out) {
+  if (!params || !out || n < 1) return fail(VEBI_ERR_ARG, "bad argument");
+  *out = nullptr;
+  auto* b = new vebi_batch();
+  for (int i = 0; i < n; ++i) {
+    vebi_ctx* c = nullptr;
+    int st = vebi_create(params + i, &c);
+    if (st) {
+      std::string m = g_err;
+      vebi_batch_destroy(b);
+      return fail(st, "batch instance " + std::to_string(i) + ": " + m);
+    }
+    b->ctx.push_back(c);
+  }
+  *out = b;
+  return VEBI_OK;
+}
+
+int vebi_batch_get(vebi_batch* b, int32_t i, vebi_ctx** ctx) {
+  if (!b || !ctx || i < 0 || i >= (int)b->ctx.size()) return fail(VEBI_ERR_ARG, "bad argument");
+  *ctx = b->ctx[i];
+  return VEBI_OK;
+}
+
+int vebi_batch_step(vebi_batch* b, int32_t nsteps, double* ms, vebi_step_stats* stats) {
+  if (!b || nsteps < 0) return fail(VEBI_ERR_ARG, "bad argument");
+  const int n = (int)b->ctx.size();
+  for (int i = 0; i < n; ++i) {
+    Ctx& x = b->ctx[i]->x;
+    if (!x.have_state) return fail(VEBI_ERR_ARG, "batch instance without state");
+  }
+  const bool graph = batch_graph_ready(b);
+  cudaStream_t s0 = b->ctx[0]->x.st;
+  // every instance's pending work (uploads) is ordered before the batch; the whole batch
+  // runs on instance 0's stream when it is one graph, else on the instances' own streams
+  std::vector<cudaEvent_t> ev(n);
+  for (int i = 0; i < n; ++i) cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
+  for (int i = 0; i < n; ++i) {
+    Ctx& x = b->ctx[i]->x;
+    x.launches = 0;
+    cudaMemsetAsync(&x.d.s->ls_iters_total, 0, sizeof(int), x.st);
+    if (i) {
+      cudaEventRecord(ev[i], x.st);
+      cudaStreamWaitEvent(s0, ev[i], 0);
+    }
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, s0);
+  if (graph) {
+    for (int s = 0; s < nsteps; ++s) cudaGraphLaunch(b->graph, s0);
+  } else {
+    for (int i = 1; i < n; ++i) cudaStreamWaitEvent(b->ctx[i]->x.st, e0, 0);
+    for (int s = 0; s < nsteps; ++s)
+      for (int i = 0; i < n; ++i) {
+        Ctx& x = b->ctx[i]->x;
+        const bool timing = x.timing;
+        x.timing = false;
+        launch_step(x, 0);
+        x.timing = timing;
+      }
+    for (int i = 1; i < n; ++i) {
+      cudaEventRecord(ev[i], b->ctx[i]->x.st);
+      cudaStreamWaitEvent(s0, ev[i], 0);
+    }
+  }
+  cudaEventRecord(e1, s0);
+  cudaError_t se = cudaStreamSynchronize(s0);
+  int st = VEBI_OK;
+  if (se != cudaSuccess) st = fail(VEBI_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString(se));
+  int n_failed = 0, first_failed = -1;
+  for (int i = 0; i < n && st == VEBI_OK; ++i) {
+    Ctx& x = b->ctx[i]->x;
+    const bool timing = x.timing;
+    x.timing = false;
+    vebi_step_stats o;
+    int si = finish_step(x, &o, true);
+    x.timing = timing;
+    o.nsteps = nsteps;
+    o.gpu_launches = graph ? b->launches[i] * nsteps : x.launches;
+    if (si && !o.error) o.error = si;  // a failure seen only on the host (all liquid binned)
+    if (stats) stats[i] = o;
+    if (si == VEBI_ERR_CUDA) st = si;
+    else if (si) {
+      ++n_failed;
+      if (first_failed < 0) first_failed = i;
+    }
+  }
+  if (st == VEBI_OK && n_failed)
+    g_err = std::to_string(n_failed) + " instance(s) failed, first " + std::to_string(first_failed) +
+            " (status in stats[i].error)";
+  else if (st == VEBI_OK)
+    g_err.clear();
+  float t = 0.f;
+  cudaEventElapsedTime(&t, e0, e1);
+  if (ms) *ms = t;
+  for (int i = 0; i < n; ++i) cudaEventDestroy(ev[i]);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return st;
+}
+
+int vebi_batch_destroy(vebi_batch* b) {
+  if (!b) return VEBI_OK;
+  batch_drop_graph(b);
+  for (auto* c : b->ctx) vebi_destroy(c);
+  delete b;
   return VEBI_OK;
 }
 

@@ -69,6 +69,7 @@ struct Scal {
   unsigned int bar_gen;
   int refine_iters;
   int ls_iters_total;                // summed over the steps of one vebi_run_steps call
+  int first_error;                   // first failing status since the last upload (sticky)
 };
 
 // Device arrays of one context.  Particle fields have capacity cap = npfb + mcap and are

@@ -29,6 +29,8 @@ struct Ctx {
   bool graph_used[2][VEBI_NSTAGES] = {};
   int coop_blocks = 0;       // persistent PPE grid (co-resident blocks)
   int coop_blocks_mixed = 0; // same for the mixed-precision solver
+  int solver_rows_per_thread = 1;  // batch tuning: rows per solver thread
+  int grid_gen = 0;                // bumped when a launch shape changes (captured graphs are stale)
   int gs_blocks = 0;         // grid of grid-stride kernels over dynamic counts
   int sel_max_blocks = 0;    // blocks of the ordered-select kernels
   int precision = VEBI_PREC_FP64;

@@ -18,7 +18,13 @@
 namespace vebi {
 
 // ------------------------------------------------------------------------------- step start
-__global__ void k_step_reset(Scal* s, int npfb) {
+__global__ void k_step_reset(Scal* s, int npfb, int nbS) {
+  // a failed step (device status, or every liquid particle binned) stays recorded; later
+  // steps of this state skip the PPE solve
+  if (!s->first_error) {
+    if (s->error) s->first_error = s->error;
+    else if (npfb > nbS && s->n_inbin == npfb - nbS) s->first_error = VEBI_ERR_ALL_IN_BIN;
+  }
   s->umax_bits = (unsigned long long)__double_as_longlong(1.0e-10);
   s->maxU_bits = (unsigned long long)__double_as_longlong(1.0e-10);
   s->absu_bits = s->absv_bits = s->absp_bits = 0ull;
@@ -479,7 +485,7 @@ static void run_stage(Ctx& x, int kind, int ib, int n0, int n1_static, int n_ite
 
 void launch_advect_bin(Ctx& x) {
   const Consts& c = x.c;
-  VEBI_LAUNCH(x, k_step_reset, 1, 1, x.d.s, c.npfb);
+  VEBI_LAUNCH(x, k_step_reset, 1, 1, x.d.s, c.npfb, c.nbS);
   VEBI_LAUNCH(x, k_save_umax, grid_for(c.npfb), TPB, c, x.d);
   VEBI_LAUNCH(x, k_advect_bin, grid_for(c.npfb), TPB, c, x.d);
 }

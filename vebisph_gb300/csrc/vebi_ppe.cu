@@ -228,6 +228,7 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int stride = gridDim.x * blockDim.x;
   Scal* s = a.sc;
+  if (*((volatile int*)&s->first_error)) return;  // this state already failed a step
   double* part = a.part;
   const double rinv1 = 1.0 / (1.0 + 1.0e-15);
   const double small = NONULL ? 1.0e-6 : 4.0;  // open solver: the integer expression 10-6
@@ -402,7 +403,8 @@ void launch_ppe(Ctx& x) {
   }
   // persistent cooperative launch: all blocks co-resident, so the grid barrier is safe
   int nblk = x.coop_blocks;
-  long long need = (c.npfb + TPB - 1) / TPB;
+  const long long rows_per_block = (long long)TPB * (x.solver_rows_per_thread > 0 ? x.solver_rows_per_thread : 1);
+  long long need = (c.npfb + rows_per_block - 1) / rows_per_block;
   if (need < nblk) nblk = (int)(need < 1 ? 1 : need);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nblk);
@@ -498,6 +500,7 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab_mixed(MxArgs a) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int stride = gridDim.x * blockDim.x;
   Scal* s = a.sc;
+  if (*((volatile int*)&s->first_error)) return;  // this state already failed a step
   double* part = a.part;
   const double rinv1 = 1.0 / (1.0 + 1.0e-15);
   const double small = NONULL ? 1.0e-6 : 4.0;
@@ -656,7 +659,8 @@ void launch_ppe_mixed_solve(Ctx& x) {
   const Consts& c = x.c;
   VEBI_LAUNCH(x, k_matrix_mixed, grid_for(c.npfb), TPB, c, x.d);
   int nblk = x.coop_blocks_mixed;
-  long long need = (c.npfb + TPB - 1) / TPB;
+  const long long rows_per_block = (long long)TPB * (x.solver_rows_per_thread > 0 ? x.solver_rows_per_thread : 1);
+  long long need = (c.npfb + rows_per_block - 1) / rows_per_block;
   if (need < nblk) nblk = (int)(need < 1 ? 1 : need);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nblk);

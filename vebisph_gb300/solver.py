@@ -37,16 +37,23 @@ def _dp(a):
 
 
 class StepSolver:
-    """One GPU context holding one simulation's particle state."""
+    """One GPU context holding one simulation's particle state.
 
-    def __init__(self, case: Case, precision: int = abi.PREC_FP64, timing: bool = False):
+    `handle` wraps a context owned elsewhere (an instance of a BatchSolver) instead of
+    creating one."""
+
+    def __init__(self, case: Case, precision: int = abi.PREC_FP64, timing: bool = False, handle=None):
         self.lib = abi.load_library()
         self.case = case
         self.params = case.params(precision)
         self.x_mint, self.x_maxt, self.y_mint, self.y_maxt = (
             self.params.x_mint, self.params.x_maxt, self.params.y_mint, self.params.y_maxt)
-        h = C.c_void_p()
-        self._check(self.lib.vebi_create(C.byref(self.params), C.byref(h)), "vebi_create")
+        self.owned = handle is None
+        if handle is None:
+            h = C.c_void_p()
+            self._check(self.lib.vebi_create(C.byref(self.params), C.byref(h)), "vebi_create")
+        else:
+            h = handle
         self.h = h
         if timing:
             self.lib.vebi_set_timing(self.h, 1)
@@ -107,9 +114,75 @@ class StepSolver:
                     name)
         return out
 
+    def set_solver_grid(self, rows_per_thread: int):
+        self._check(self.lib.vebi_set_solver_grid(self.h, int(rows_per_thread)), "vebi_set_solver_grid")
+
     def close(self):
         if getattr(self, "h", None):
-            self.lib.vebi_destroy(self.h)
+            if self.owned:
+                self.lib.vebi_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BatchSolver:
+    """Independent simulations of uneven sizes advanced together (vebi_batch_*): every batch
+    step replays each instance's captured step graph on its own stream; one wait per call."""
+
+    def __init__(self, cases_list, precision: int = abi.PREC_MIXED):
+        self.lib = abi.load_library()
+        n = len(cases_list)
+        arr = (abi.VebiParams * n)(*[c.params(precision) for c in cases_list])
+        h = C.c_void_p()
+        st = self.lib.vebi_batch_create(arr, n, C.byref(h))
+        if st:
+            raise VebiError(st, "vebi_batch_create", self.lib.vebi_last_error().decode())
+        self.h = h
+        self.instances = []
+        for i, c in enumerate(cases_list):
+            ch = C.c_void_p()
+            self.lib.vebi_batch_get(self.h, i, C.byref(ch))
+            self.instances.append(StepSolver(c, precision, handle=ch))
+        self.n_fluid = sum(c.n_fluid for c in cases_list)
+
+    def step(self, nsteps: int = 1):
+        """Advance every instance by nsteps; returns (device ms, per-instance stats)."""
+        n = len(self.instances)
+        stats = (abi.VebiStepStats * n)()
+        ms = C.c_double(0.0)
+        st = self.lib.vebi_batch_step(self.h, int(nsteps), C.byref(ms), stats)
+        if st:
+            raise VebiError(st, "vebi_batch_step", self.lib.vebi_last_error().decode())
+        # instances that failed carry their status in stats[i]["error"]; the others went on
+        return ms.value, [stats[i].as_dict() for i in range(n)]
+
+    def set_solver_grid(self, rows_per_thread: int):
+        for inst in self.instances:
+            inst.set_solver_grid(rows_per_thread)
+
+    def autotune(self, candidates=(1, 2, 4, 8)) -> dict:
+        """Pick the solver rows-per-thread of the batch by measurement: one step to capture the
+        graphs, one timed step per candidate (these are real steps of the simulations)."""
+        times = {}
+        for r in candidates:
+            self.set_solver_grid(r)
+            self.step(1)
+            ms, _ = self.step(1)
+            times[r] = ms
+        best = min(times, key=times.get)
+        self.set_solver_grid(best)
+        return {"rows_per_thread": best, "ms_per_candidate": times}
+
+    def close(self):
+        if getattr(self, "h", None):
+            for inst in self.instances:
+                inst.h = None
+            self.lib.vebi_batch_destroy(self.h)
             self.h = None
 
     def __del__(self):
