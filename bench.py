@@ -281,6 +281,7 @@ def run_gb300(args, dist: Dist):
         "e2e": e2e,
         "clocks": clk.summary(),
         "nmirror": st["nmirror"], "maxneighbours": st["maxneighbours"],
+        "drag": drag_summary(case, st, fields),
     }
     res["_fields"] = fields
     sol.close()
@@ -389,6 +390,19 @@ def run_batch(args, dist: Dist):
     }
 
 
+def drag_summary(case, st: dict, fields: dict):
+    """Force of the fluid on the cylinder after the last timed step (the circle-mirror pair
+    terms of the step) and the drag coefficient K = F_x / (eta0 U): eta0 = sqrt(Pr/Ra) the total
+    viscosity 1/Re, U the mean fluid x-velocity."""
+    if not case.nb_circles:
+        return None
+    fx, fy = st["circle_force"]
+    fl = slice(case.nbS, case.npfb)
+    u_mean = float(np.mean(fields["ux"][fl]))
+    eta0 = (case.Pr / case.Ra) ** 0.5
+    return {"F_x": fx, "F_y": fy, "U_mean": u_mean, "K": fx / (eta0 * u_mean)}
+
+
 def mixed_summary(f64: dict, mx: dict) -> dict:
     """Speed of the mixed step and its difference from the FP64 step after the same steps from
     the same initial state: velocity and pressure (max abs difference / max abs FP64 value),
@@ -406,6 +420,9 @@ def mixed_summary(f64: dict, mx: dict) -> dict:
             "stage_ms_per_step": mx["stage_ms_per_step"], "gpu_launches": mx["gpu_launches"],
             "rel_diff_vs_fp64": {"u": float(du), "p": float(dp), "N1_wake_max": abs(n1a - n1b) / max(abs(n1b), 1e-300)},
             "N1_wake_max": {"mixed": n1a, "fp64": n1b},
+            "drag": mx.get("drag"),
+            "drag_rel_diff_vs_fp64": (abs(mx["drag"]["F_x"] - f64["drag"]["F_x"]) / abs(f64["drag"]["F_x"])
+                                      if mx.get("drag") and f64.get("drag") else None),
             "note": ("both PPE solves stop at the 1000-iteration cap unconverged on this workload (see "
                      "LS_residual_last); on converging cases the mixed velocity stays within 1e-4 of FP64 "
                      "(tests/test_gpu_mixed.py)")}

@@ -118,6 +118,9 @@ typedef struct vebi_step_stats {
   double rms_u;         /* secondary_properties diagnostic (div_free.F90:170-183)    */
   double ppe_rhs_mean;  /* DC removed from the PPE right-hand side                   */
   double stage_ms[VEBI_NSTAGES]; /* device time of each stage (0 unless timing on)    */
+  double circle_force[2]; /* force of the fluid on the circles (cylinder), x and y: the
+                             circle-mirror pair terms of the step (no reference counterpart;
+                             0 without circles) */
   int32_t LS_iters;     /* BiCGSTAB iterations                                       */
   int32_t n_inbin;
   int32_t np, npfb, nmirror, maxneighbours;

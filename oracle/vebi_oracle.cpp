@@ -94,6 +94,8 @@ struct Oracle {
   double LS_residual = 0;
   int n_inbin = 0, n_escapees = 0, error = 0, warnings = 0;
   double ppe_rhs_mean = 0, rms_u = 0;
+  double circle_fx = 0, circle_fy = 0;     // force of the fluid on the circles (diagnostic)
+  std::vector<double> circ_s1, circ_s2;    // circle-mirror share of the predictor sums
   int maxneighbours = 0;
   double t_solve_ms = 0.0, t_step_ms = 0.0;  // per-step wall times (CPU baseline)
   static double wtime() {
@@ -1120,6 +1122,32 @@ struct Oracle {
       }
       rh1[i] = s1; rh2[i] = s2; rht[i] = st;
     }
+    // the circle mirrors' share of the same sums (the drag diagnostic; no reference counterpart)
+    circ_s1.assign(npfb, 0.0); circ_s2.assign(npfb, 0.0);
+    if (P.nb_circles > 0) {
+#pragma omp parallel for schedule(static)
+      for (int i = nbS; i < npfb; ++i) {
+        double s1 = 0, s2 = 0;
+        M2 Kc = K(i);
+        for (int k = 0; k < ij_count[i]; ++k) {
+          int j = L(k, i);
+          if (j < npfb || vrelation[j] <= 999) continue;
+          double u1 = ux[i] - ux[j], u2 = uy[i] - uy[j];
+          double w1 = wGx[E(k, i)], w2 = wGy[E(k, i)], wl = wL[E(k, i)];
+          if (P.const_mod == 1) {
+            s1 = s1 + cs * u1 * wl;
+            s2 = s2 + cs * u2 * wl;
+          } else {
+            double T11 = tau[0][j] - tau[0][i], T21 = tau[1][j] - tau[1][i];
+            double T12 = tau[2][j] - tau[2][i], T22 = tau[3][j] - tau[3][i];
+            double kw1 = Kc.a11 * w1 + Kc.a12 * w2, kw2 = Kc.a21 * w1 + Kc.a22 * w2;
+            s1 = s1 + cp * (T11 * kw1 + T12 * kw2) + cs * u1 * wl;
+            s2 = s2 + cp * (T21 * kw1 + T22 * kw2) + cs * u2 * wl;
+          }
+        }
+        circ_s1[i] = s1; circ_s2[i] = s2;
+      }
+    }
     for (int i = 0; i < npfb; ++i) rh2[i] = rh2[i] + theta[i];  // buoyancy (:111-119)
     for (int i = nbS; i < npfb; ++i) {
       ux[i] = ux[i] + rh1[i] * dt;
@@ -1318,6 +1346,29 @@ struct Oracle {
       gpx[i] = Kc.a11 * a + Kc.a12 * b;
       gpy[i] = Kc.a21 * a + Kc.a22 * b;
     }
+    // force of the fluid on the circles: per fluid particle, dv x (circle-mirror share of the
+    // pressure gradient - circle-mirror share of the viscous/polymeric sums)
+    circle_fx = circle_fy = 0.0;
+    if (P.nb_circles > 0) {
+      std::vector<double> fx(npfb, 0.0), fy(npfb, 0.0);
+#pragma omp parallel for schedule(static)
+      for (int i = nbS; i < npfb; ++i) {
+        if (inbin[i]) continue;
+        double a = 0, b = 0;
+        for (int k = 0; k < ij_count[i]; ++k) {
+          int j = L(k, i);
+          if (j < npfb || vrelation[j] <= 999) continue;
+          double temp = p[j] - p[i];
+          a = a + temp * wGx[E(k, i)];
+          b = b + temp * wGy[E(k, i)];
+        }
+        M2 Kc = K(i);
+        fx[i] = P.dv * ((Kc.a11 * a + Kc.a12 * b) - circ_s1[i]);
+        fy[i] = P.dv * ((Kc.a21 * a + Kc.a22 * b) - circ_s2[i]);
+      }
+      circle_fx = chunk_sum(0, npfb, [&](int64_t i) { return fx[i]; });
+      circle_fy = chunk_sum(0, npfb, [&](int64_t i) { return fy[i]; });
+    }
   }
 
   // correct_velocity (correct_velocity.F90:13-70): remove the velocity component of particles
@@ -1468,6 +1519,7 @@ struct Oracle {
     }
     s->max_abs_u = mu; s->max_abs_v = mv; s->max_abs_p = mp;
     s->rms_u = rms_u; s->ppe_rhs_mean = ppe_rhs_mean;
+    s->circle_force[0] = circle_fx; s->circle_force[1] = circle_fy;
     s->LS_iters = LS_iters; s->n_inbin = n_inbin; s->np = np; s->npfb = npfb;
     s->nmirror = nmirror; s->maxneighbours = maxneighbours; s->n_escapees = n_escapees;
     s->error = error; s->warnings = warnings;

@@ -52,6 +52,14 @@ def test_one_step_parity(libs, name):
         for nm in ("conc", "div_r"):
             a, b = gpu.get(nm), ref.get(nm)
             assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max(), nm
+    # force on the circles (drag/lift diagnostic): pair terms with the new pressure, so the
+    # pressure tolerance applies, relative to the force's magnitude
+    if case.nb_circles:
+        fg, fo = np.array(sg["circle_force"]), np.array(so["circle_force"])
+        assert np.abs(fo).max() > 0
+        assert np.abs(fg - fo).max() <= 1e-5 * np.abs(fo).max(), (fg, fo)
+    else:
+        assert sg["circle_force"] == [0.0, 0.0]
     # vorticity diagnostic (secondary_properties) follows the final velocity
     v_g, v_o = gpu.get("vort"), ref.get("vort")
     assert np.abs(v_g - v_o).max() <= 1e-5 * max(np.abs(v_o).max(), 1e-30)

@@ -39,12 +39,14 @@ def test_dist_collectives_world2(tmp_path):
         "d = bench.Dist()\n"
         "d.barrier()\n"
         "mx = d.max(float(d.rank + 1)); sm = d.sum(10.0)\n"
-        "print(json.dumps({'rank': d.rank, 'world': d.world, 'max': mx, 'sum': sm}))\n"
-        "d.close()\n" % str(ROOT))
+        "out = {'rank': d.rank, 'world': d.world, 'max': mx, 'sum': sm}\n"
+        "open(%r + '/rank%%d.json' %% d.rank, 'w').write(json.dumps(out))\n"
+        "d.close()\n" % (str(ROOT), str(tmp_path)))
     r = _torchrun([str(code)])
     assert r.returncode == 0, r.stderr[-2000:]
-    outs = [json.loads(ln) for ln in r.stdout.splitlines() if ln.startswith("{")]
-    assert len(outs) == 2
+    # one file per rank: the ranks' stdout lines can interleave
+    outs = [json.loads((tmp_path / f"rank{k}.json").read_text()) for k in range(2)]
+    assert sorted(o["rank"] for o in outs) == [0, 1]
     for o in outs:
         assert o["world"] == 2 and o["max"] == 2.0 and o["sum"] == 20.0
 

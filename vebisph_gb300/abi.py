@@ -67,6 +67,7 @@ class VebiStepStats(C.Structure):
         ("max_abs_u", C.c_double), ("max_abs_v", C.c_double), ("max_abs_p", C.c_double),
         ("rms_u", C.c_double), ("ppe_rhs_mean", C.c_double),
         ("stage_ms", C.c_double * NSTAGES),
+        ("circle_force", C.c_double * 2),
         ("LS_iters", C.c_int32), ("n_inbin", C.c_int32),
         ("np", C.c_int32), ("npfb", C.c_int32), ("nmirror", C.c_int32), ("maxneighbours", C.c_int32),
         ("n_escapees", C.c_int32), ("error", C.c_int32), ("warnings", C.c_int32),
@@ -78,7 +79,7 @@ class VebiStepStats(C.Structure):
         d = {}
         for name, _ in self._fields_:
             v = getattr(self, name)
-            d[name] = list(v) if name == "stage_ms" else v
+            d[name] = list(v) if name in ("stage_ms", "circle_force") else v
         return d
 
 

@@ -223,7 +223,7 @@ static int allocate_all(Ctx& x) {
   A_(d.bs, n); A_(d.bsi, n); A_(d.bt, n); A_(d.bM, n);
   size_t np_part = (size_t)grid_for(c.npfb);
   size_t coop_part = (size_t)x.coop_blocks * 12;
-  A_(d.partials, (np_part > coop_part ? np_part : coop_part) + 64);
+  A_(d.partials, (2 * np_part > coop_part ? 2 * np_part : coop_part) + 64);
   A_(d.gpx, n); A_(d.gpy, n);
   if (x.precision == VEBI_PREC_MIXED) {
     A_(d.ppe_val32, E); A_(d.rowsum, n); A_(d.pi2, n); A_(d.si2, n);
@@ -330,6 +330,8 @@ static int finish_step(Ctx& x, vebi_step_stats* stats, bool sync) {
   o.max_abs_v = bits_to_double_host(s.absv_bits);
   o.max_abs_p = bits_to_double_host(s.absp_bits);
   o.rms_u = s.rms_u;
+  o.circle_force[0] = s.circle_fx;
+  o.circle_force[1] = s.circle_fy;
   o.ppe_rhs_mean = s.rhs_mean;
   o.LS_iters = s.ls_iters;
   o.n_inbin = s.n_inbin;

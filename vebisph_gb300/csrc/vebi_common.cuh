@@ -54,6 +54,7 @@ struct Scal {
   double rhs_mean;
   double ls_residual;
   double rms_u;
+  double circle_fx, circle_fy;       // force of the fluid on the circles (k_circle_force)
   int nmirror;                       // mirror counter `imp`
   int np;
   int n_inbin;

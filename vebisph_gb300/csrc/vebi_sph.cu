@@ -464,6 +464,75 @@ __global__ void k_secondary_final(Consts c, Dev d, int nblk) {
   if (threadIdx.x == 0) d.s->rms_u = sqrt(s / (double)c.npfb);
 }
 
+// Force of the fluid on the circles (the cylinder's drag and lift), as the step's own pair
+// terms see it: for every fluid particle, the circle mirrors' (vrelation > 999) share of the
+// viscous and polymeric sums of prediction_step (predictor_mod.F90:27-139) and of the pressure
+// gradient of calc_pressure_gradient (gradient_calculation.F90:16-48), times dv; the circles
+// feel the opposite.  Evaluated after the step from the values those stages read: the
+// start-of-step fluid velocity u0, the mirrors' creation-time velocity (ux/uy at npfb..), the
+// updated tau and the new pressure.  A diagnostic of this library; the reference has none.
+template <class W>
+__global__ void k_circle_force(Consts c, Dev d, const W* __restrict__ wgx, const W* __restrict__ wgy,
+                               const W* __restrict__ wl_, const W* __restrict__ k11, const W* __restrict__ k21,
+                               const W* __restrict__ k12, const W* __restrict__ k22) {
+  __shared__ double sh[TPB / 32 + 1];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double fx = 0.0, fy = 0.0;
+  if (i >= c.nbS && i < c.npfb && !d.inbin[i]) {
+    const bool ve = c.const_mod != 1;
+    const double ui = d.u0x[i], vi = d.u0y[i], pi_ = d.p[i];
+    const double K11 = (double)k11[i], K21 = (double)k21[i], K12 = (double)k12[i], K22 = (double)k22[i];
+    double Ti11 = 0, Ti21 = 0, Ti12 = 0, Ti22 = 0;
+    if (ve) { Ti11 = d.tau[0][i]; Ti21 = d.tau[1][i]; Ti12 = d.tau[2][i]; Ti22 = d.tau[3][i]; }
+    const double cs = c.coeff_solvent, cp = c.coeff_polymeric;
+    double s1 = 0, s2 = 0, a = 0, b = 0;
+    const int cnt = d.ij_count[i];
+    for (int k = 0; k < cnt; ++k) {
+      int j = d.ij_link[ELL(k, i)];
+      if (j < c.npfb || d.vrel[j] <= 999) continue;
+      double w1 = (double)wgx[ELL(k, i)], w2 = (double)wgy[ELL(k, i)], wl = (double)wl_[ELL(k, i)];
+      double u1 = ui - d.ux[j], u2 = vi - d.uy[j];
+      if (ve) {
+        double T11 = d.tau[0][j] - Ti11, T21 = d.tau[1][j] - Ti21;
+        double T12 = d.tau[2][j] - Ti12, T22 = d.tau[3][j] - Ti22;
+        double kw1 = K11 * w1 + K12 * w2, kw2 = K21 * w1 + K22 * w2;
+        s1 = s1 + cp * (T11 * kw1 + T12 * kw2) + cs * u1 * wl;
+        s2 = s2 + cp * (T21 * kw1 + T22 * kw2) + cs * u2 * wl;
+      } else {
+        s1 = s1 + cs * u1 * wl;
+        s2 = s2 + cs * u2 * wl;
+      }
+      double temp = d.p[j] - pi_;
+      a = a + temp * w1;
+      b = b + temp * w2;
+    }
+    const double gx = K11 * a + K12 * b, gy = K21 * a + K22 * b;
+    fx = c.dv * (gx - s1);
+    fy = c.dv * (gy - s2);
+  }
+  double bx = block_sum<TPB>(fx, sh);
+  double by = block_sum<TPB>(fy, sh);
+  if (threadIdx.x == 0) {
+    d.partials[blockIdx.x] = bx;
+    d.partials[gridDim.x + blockIdx.x] = by;
+  }
+}
+
+__global__ void k_circle_force_final(Dev d, int nblk) {
+  __shared__ double sh[TPB / 32 + 1];
+  double sx = 0.0, sy = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+    sx += d.partials[b];
+    sy += d.partials[nblk + b];
+  }
+  sx = block_sum<TPB>(sx, sh);
+  sy = block_sum<TPB>(sy, sh);
+  if (threadIdx.x == 0) {
+    d.s->circle_fx = sx;
+    d.s->circle_fy = sy;
+  }
+}
+
 void launch_prep_weights32(Ctx& x);
 void launch_shift32(Ctx& x);
 void launch_gradients32(Ctx& x);
@@ -530,6 +599,15 @@ void launch_final(Ctx& x, int secondary) {
   if (c.correct_velocity) {
     VEBI_LAUNCH(x, k_correct_velocity, g, TPB, c, x.d);
     VEBI_LAUNCH(x, k_advect_final, g, TPB, c, x.d);
+  }
+  if (c.ncirc > 0) {
+    if (mixed)
+      VEBI_LAUNCH(x, k_circle_force<float>, g, TPB, c, x.d, x.d.wGx32, x.d.wGy32, x.d.wL32, x.d.kgcm32[0],
+                  x.d.kgcm32[1], x.d.kgcm32[2], x.d.kgcm32[3]);
+    else
+      VEBI_LAUNCH(x, k_circle_force<double>, g, TPB, c, x.d, x.d.wGx, x.d.wGy, x.d.wL, x.d.kgcm[0], x.d.kgcm[1],
+                  x.d.kgcm[2], x.d.kgcm[3]);
+    VEBI_LAUNCH(x, k_circle_force_final, 1, TPB, x.d, g);
   }
   if (secondary) {
     stage_mark(x, 13);
