@@ -186,6 +186,7 @@ def run_gb300(args, dist: Dist):
     if args.itermax:
         case.itermax = args.itermax
     case.ppe_warm_start = 1 if args.warm_start else 0
+    case.ppe_precond = abi.PRECOND_MULTIGRID if args.precond == "multigrid" else abi.PRECOND_NONE
     prec = abi.PREC_MIXED if args.precision == "mixed" else abi.PREC_FP64
     sol = StepSolver(case, precision=prec, timing=True)
     n_fluid = case.n_fluid
@@ -475,6 +476,8 @@ def main():
     ap.add_argument("--wi", type=float, default=0.6)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--precond", choices=["none", "multigrid"], default="none",
+                    help="opt-in PPE preconditioner (none = the reference's solver)")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-iters", type=int, default=20, help="BiCGSTAB cap of the CPU sample")
     ap.add_argument("--ref-iters", type=float, default=1001.0,

@@ -63,6 +63,16 @@ enum {
   VEBI_PREC_MIXED = 1   /* FP32 pair sums/SpMV, FP64 PPE refinement and eigen-step           */
 };
 
+/* PPE preconditioner.  NONE is the reference (closed domains unpreconditioned,
+ * linear_solver.F90:318; open domains Jacobi, :82-227).  MULTIGRID (opt-in) applies one
+ * aggregation-multigrid V-cycle on the cell grid per preconditioning step: the solver stops on
+ * the same residual test and reaches the same solution within its tolerance, in far fewer
+ * iterations; results differ from the reference's by that tolerance. */
+enum {
+  VEBI_PRECOND_NONE = 0,
+  VEBI_PRECOND_MULTIGRID = 1
+};
+
 /*
  * Run parameters.  Field meanings follow INDAT (source/base/input.F90:18-38) and
  * IBOUND (input.F90:51-81).  Patch and circle arrays are 0-based copies of the
@@ -105,7 +115,8 @@ typedef struct vebi_params {
                                           has the call commented out (div_free.F90:105)          */
   int32_t ppe_warm_start;              /* 1: start BiCGSTAB from the previous step's P instead of
                                           x0 = 0 (ppe...:145); changes results, off by default   */
-  int32_t reserved[5];
+  int32_t ppe_precond;                 /* VEBI_PRECOND_*: preconditioner of the PPE BiCGSTAB     */
+  int32_t reserved[4];
 } vebi_params;
 
 /* Per-step scalars the Fortran driver and `output` read after div_free

@@ -1,0 +1,66 @@
+"""The opt-in multigrid-preconditioned PPE (VEBI_PRECOND_MULTIGRID) against the oracle, which
+runs the reference's unpreconditioned BiCGSTAB: both stop on the same residual test, so on
+cases the reference solves within its iteration cap the fields agree within the FP64 parity
+tolerances, in far fewer iterations."""
+import numpy as np
+import pytest
+
+from tests.parity import TOL, relerr
+from vebisph_gb300 import abi, cases
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "poiseuille40": lambda: cases.poiseuille(40, seed=1),
+    "rb_deck": cases.rayleigh_benard_deck,
+    "cylinder20k": lambda: cases.cylinder(2.0e4, Wi=0.6, seed=2),
+    "cavity64": lambda: cases.cavity(64, seed=3),
+    "free_surface_open": lambda: cases.free_surface_periodic(75, seed=5),
+}
+
+
+def _mg(case):
+    case.ppe_precond = abi.PRECOND_MULTIGRID
+    return case
+
+
+@pytest.fixture(scope="module")
+def libs(built):
+    from oracle.oracle import OracleSolver
+    from vebisph_gb300.solver import StepSolver
+    return StepSolver, OracleSolver
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_multigrid_step_matches_oracle(libs, name):
+    StepSolver, OracleSolver = libs
+    gpu, ref = StepSolver(_mg(CASES[name]())), OracleSolver(CASES[name]())
+    n = gpu.case.npfb
+    for step in range(3):
+        sg, so = gpu.step(), ref.step()
+        assert sg["error"] == 0 and not (sg["warnings"] & abi.WARN_MAXITER)
+        if so["LS_iters"] > 30:
+            assert sg["LS_iters"] < so["LS_iters"], (sg["LS_iters"], so["LS_iters"])
+        scale_p = max(np.abs(ref.get("p")[:n]).max(), 1e-30)
+        assert relerr(gpu.get("p")[:n], ref.get("p")[:n], scale_p) <= TOL["p"], step
+        us = max(np.abs(ref.get("ux")[:n]).max(), np.abs(ref.get("uy")[:n]).max(), 1e-30)
+        for nm in ("ux", "uy"):
+            assert relerr(gpu.get(nm)[:n], ref.get(nm)[:n], us) <= TOL[nm], (step, nm)
+    if gpu.case.i_open_domain == 0:  # the zero mean of the reference's iterates is kept
+        p = gpu.get("p")[:n]
+        assert abs(p.mean()) <= 1e-9 * np.abs(p).max()
+    gpu.close()
+    ref.close()
+
+
+def test_multigrid_is_deterministic(libs):
+    StepSolver, _ = libs
+    out = []
+    for _ in range(2):
+        s = StepSolver(_mg(cases.cylinder(2.0e4, Wi=0.6, seed=2)))
+        for _ in range(2):
+            st = s.step()
+        out.append((st["LS_iters"], s.get("p").copy(), s.get("ux").copy()))
+        s.close()
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1]) and np.array_equal(out[0][2], out[1][2])

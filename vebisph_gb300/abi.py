@@ -31,6 +31,8 @@ WARN_BICGSTAB_BREAKDOWN = 1
 WARN_MAXITER = 2
 WARN_ESCAPEES = 4
 PREC_FP64 = 0
+PRECOND_NONE = 0
+PRECOND_MULTIGRID = 1
 PREC_MIXED = 1
 
 _D2P = C.c_double * 2 * MAX_PATCHES
@@ -57,7 +59,8 @@ class VebiParams(C.Structure):
         ("npfb", C.c_int32), ("nbS", C.c_int32),
         ("const_mod", C.c_int32), ("itermax", C.c_int32), ("nplink", C.c_int32),
         ("nmirror_cap", C.c_int32), ("precision", C.c_int32), ("correct_velocity", C.c_int32),
-        ("ppe_warm_start", C.c_int32), ("reserved", C.c_int32 * 5),
+        ("ppe_warm_start", C.c_int32), ("ppe_precond", C.c_int32),
+        ("reserved", C.c_int32 * 4),
     ]
 
 

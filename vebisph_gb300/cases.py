@@ -69,6 +69,7 @@ class Case:
     nmirror_cap: int = 0
     correct_velocity: int = 0
     ppe_warm_start: int = 0
+    ppe_precond: int = 0
 
     def __post_init__(self):
         n = self.npfb
@@ -137,6 +138,7 @@ class Case:
         p.precision = precision
         p.correct_velocity = self.correct_velocity
         p.ppe_warm_start = self.ppe_warm_start
+        p.ppe_precond = self.ppe_precond
         return p
 
     def fortran_planes(self, ld: int | None = None) -> dict:

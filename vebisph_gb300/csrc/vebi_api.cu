@@ -12,6 +12,8 @@ namespace vebi {
 
 int ppe_solver_blocks(int device, int nsm);
 int ppe_mixed_blocks(int nsm);
+int ppe_mg_blocks(int nsm);
+std::vector<int> mg_level_dims(int gx, int gy);
 
 static thread_local std::string g_err;
 
@@ -101,6 +103,7 @@ static int build_consts(Ctx& x) {
   c.const_mod = P.const_mod == 1 ? 1 : 2;
   c.correct_velocity = P.correct_velocity ? 1 : 0;
   c.warm_start = P.ppe_warm_start ? 1 : 0;
+  c.precond = P.ppe_precond == VEBI_PRECOND_MULTIGRID ? 1 : 0;
   c.npfb = P.npfb;
   c.nbS = P.nbS;
   for (int i = 0; i < nb; ++i) {
@@ -222,13 +225,33 @@ static int allocate_all(Ctx& x) {
   A_(d.bx, n); A_(d.br, n); A_(d.brb, n); A_(d.bv, n); A_(d.bp, n); A_(d.bpi, n);
   A_(d.bs, n); A_(d.bsi, n); A_(d.bt, n); A_(d.bM, n);
   size_t np_part = (size_t)grid_for(c.npfb);
-  size_t coop_part = (size_t)x.coop_blocks * 12;
+  // block partials of the persistent solvers: 12 slots of one value per block
+  int part_blocks = x.coop_blocks;
+  if (x.coop_blocks_mixed > part_blocks) part_blocks = x.coop_blocks_mixed;
+  if (x.mg_blocks > part_blocks) part_blocks = x.mg_blocks;
+  size_t coop_part = (size_t)part_blocks * 12;
   A_(d.partials, (2 * np_part > coop_part ? 2 * np_part : coop_part) + 64);
   A_(d.gpx, n); A_(d.gpy, n);
   if (x.precision == VEBI_PREC_MIXED) {
     A_(d.ppe_val32, E); A_(d.rowsum, n); A_(d.pi2, n); A_(d.si2, n);
     A_(d.wGx32, E); A_(d.wGy32, E); A_(d.wL32, E);
     for (int q = 0; q < 4; ++q) A_(d.kgcm32[q], n);
+  }
+  if (c.precond) {  // multigrid levels on the cell grid
+    std::vector<int> dims = mg_level_dims(c.ncx, c.ncy);
+    for (size_t l = 0; l + 1 < dims.size(); l += 2) {
+      MgLevel L{};
+      L.gx = dims[l];
+      L.gy = dims[l + 1];
+      L.n = L.gx * L.gy;
+      const size_t ln = (size_t)L.n;
+      A_(L.cnt, ln); A_(L.col, ln * MG_SLOTS); A_(L.val, ln * MG_SLOTS);
+      A_(L.diag, ln); A_(L.dinv, ln); A_(L.x, ln); A_(L.b, ln); A_(L.r, ln);
+      x.mg.push_back(L);
+    }
+    A_(x.d_mg, x.mg.size());
+    cudaMemcpy(x.d_mg, x.mg.data(), sizeof(MgLevel) * x.mg.size(), cudaMemcpyHostToDevice);
+    A_(x.mg_z, n); A_(x.mg_fr, n); A_(x.mg_dinv0, n); A_(x.mg_rsum, n);
   }
 #undef A_
   return VEBI_OK;
@@ -268,8 +291,8 @@ int vebi_create(const vebi_params* params, vebi_ctx** out) {
   cudaDeviceGetAttribute(&x.nsm, cudaDevAttrMultiProcessorCount, x.device);
   x.coop_blocks = ppe_solver_blocks(x.device, x.nsm);
   x.coop_blocks_mixed = ppe_mixed_blocks(x.nsm);
-  if (x.coop_blocks_mixed > x.coop_blocks) x.coop_blocks = x.coop_blocks_mixed;  // partials sizing
   x.gs_blocks = x.nsm * 8;
+  x.mg_blocks = ppe_mg_blocks(x.nsm);
   if (cudaStreamCreateWithFlags(&x.st, cudaStreamNonBlocking) != cudaSuccess) {
     delete h;
     return fail(VEBI_ERR_CUDA, "cudaStreamCreate failed");

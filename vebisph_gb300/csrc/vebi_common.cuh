@@ -43,6 +43,7 @@ struct Consts {
   int open_domain, shift_coeff, const_mod, itermax;
   int correct_velocity;                             // run correct_velocity (off in the reference)
   int warm_start;                                   // PPE starts from the previous P (opt-in)
+  int precond;                                      // 1: multigrid-preconditioned PPE (opt-in)
 };
 
 // Scalars that change during a step; they live in device memory so no step needs a host sync.
@@ -71,6 +72,28 @@ struct Scal {
   int refine_iters;
   int ls_iters_total;                // summed over the steps of one vebi_run_steps call
   int first_error;                   // first failing status since the last upload (sticky)
+  int mg_fail;                       // multigrid set-up overflowed a coarse row: solve without it
+};
+
+// multigrid preconditioner (opt-in): coarse-row capacity, coarsest size, level cap, levels run
+// by one block, coarsest sweeps, Jacobi damping, coarse-correction scaling
+constexpr int MG_SLOTS = 24;
+constexpr int MG_COARSEST = 2048;
+constexpr int MG_MAX_LEVELS = 12;
+constexpr int MG_BLOCK_ROWS = 8192;
+constexpr int MG_SWEEPS = 8;
+constexpr double MG_OMEGA = 0.8;
+constexpr double MG_GAMMA = 1.8;
+
+// One coarse level of the multigrid preconditioner: the cell grid (level 1) or a 2x2
+// agglomeration of the level below, as a gx x gy grid of aggregates; its Galerkin matrix in
+// ELL form (off-diagonal slots [t][c], stride n) with the diagonal apart; work vectors.
+struct MgLevel {
+  int n, gx, gy;
+  int* cnt;
+  int* col;
+  double *val, *diag, *dinv;
+  double *x, *b, *r;
 };
 
 // Device arrays of one context.  Particle fields have capacity cap = npfb + mcap and are

@@ -35,6 +35,11 @@ struct Ctx {
   int sel_max_blocks = 0;    // blocks of the ordered-select kernels
   int precision = VEBI_PREC_FP64;
   bool have_state = false;
+  // multigrid-preconditioned PPE (opt-in)
+  std::vector<MgLevel> mg;         // coarse levels, finest first
+  MgLevel* d_mg = nullptr;         // device copy of the level descriptors
+  int mg_blocks = 0;               // co-resident blocks of the preconditioned solver
+  double *mg_z = nullptr, *mg_fr = nullptr, *mg_dinv0 = nullptr, *mg_rsum = nullptr;
   std::vector<void*> allocs;
   vebi_step_stats last{};
 };

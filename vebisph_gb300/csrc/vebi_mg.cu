@@ -1,0 +1,470 @@
+// vebi_mg.cu -- opt-in multigrid preconditioner of the PPE BiCGSTAB (VEBI_PRECOND_MULTIGRID).
+// No counterpart in the reference, which solves closed domains unpreconditioned
+// (SPARSE_PBICGSTAB_nonull, linear_solver.F90:275-425, M = 1 at :318) and open domains with
+// Jacobi (SPARSE_PBICGSTAB, :82-227).
+//
+// Hierarchy.  Level 1 aggregates the particles by the cell they sit in: the cell grid of
+// cell_griddin.F90:13-24, whose cell lists the neighbour search built this step.  Each further
+// level agglomerates 2x2 aggregates of the level below, until at most MG_COARSEST remain.
+// Interpolation is piecewise constant, so a coarse matrix is the Galerkin product R A P: the
+// sum of the couplings between two aggregates.  Coarse matrices are ELL with at most MG_SLOTS
+// off-diagonal slots per row (the 3x3 neighbourhood plus partners across periodic boundaries);
+// a row that needs more sets mg_fail, and that step solves without the preconditioner.
+//
+// V-cycle, one per preconditioning step: one damped Jacobi sweep (MG_OMEGA) from zero, the
+// residual, restriction (the sum over each aggregate), the coarser levels, prolongation scaled
+// by MG_GAMMA (over-correction for piecewise-constant interpolation), one post-smoothing sweep.
+// The coarsest level takes MG_SWEEPS Jacobi sweeps.  Levels of at most MG_BLOCK_ROWS rows run in
+// block 0 alone with block barriers.  Every sum runs in a fixed order.
+//
+// Solver.  BiCGSTAB with right preconditioning, in the persistent cooperative kernel of the
+// unpreconditioned solver: the same recurrences, residual test and, for closed domains, mean
+// removal.  The preconditioned directions are made mean-free, so the solution keeps the zero
+// mean of the reference's iterates.  The V-cycle reads only its own rows of the vector it is
+// applied to, so it needs no barrier before it.
+#include "vebi_solver.cuh"
+
+namespace vebi {
+
+#define ELL(k, i) ((size_t)(k) * c.npfb + (i))
+
+// ---------------------------------------------------------------- set-up (every step)
+// add v to column `col` of a row's slot table; false when the table is full
+__device__ __forceinline__ bool slot_add(int* tc, double* tv, int& m, int col, double v) {
+  int t = 0;
+  while (t < m && tc[t] != col) ++t;
+  if (t == m) {
+    if (m == MG_SLOTS) return false;
+    tc[m] = col;
+    tv[m] = 0.0;
+    ++m;
+  }
+  tv[t] += v;
+  return true;
+}
+
+__device__ __forceinline__ void slot_store(const MgLevel& L, int row, const int* tc, const double* tv, int m,
+                                           double dg) {
+  for (int t = 0; t < m; ++t) {
+    L.col[(size_t)t * L.n + row] = tc[t];
+    L.val[(size_t)t * L.n + row] = tv[t];
+  }
+  L.cnt[row] = m;
+  L.diag[row] = dg;
+  L.dinv[row] = dg != 0.0 ? 1.0 / dg : 0.0;
+}
+
+// level 1: one thread per cell sums the PPE rows of the cell's particles (ascending index)
+__global__ void k_mg_level1(Consts c, Dev d, MgLevel L) {
+  const int cc = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cc >= L.n) return;
+  int tc[MG_SLOTS];
+  double tv[MG_SLOTS];
+  int m = 0;
+  double dg = 0.0;
+  bool ok = true;
+  const int s0 = d.cell_start[cc], ne = d.cell_cnt[cc];
+  for (int q = 0; q < ne; ++q) {
+    const int i = d.ip[s0 + q];
+    if (i >= c.npfb) break;  // mirrors follow the particles in a sorted cell list
+    dg += d.ppe_diag[i];
+    const int cnt = d.ij_count[i];
+    for (int k = 0; k < cnt; ++k) {
+      const int a = d.cellpart[d.ppe_col[ELL(k, i)]];
+      const double v = d.ppe_val[ELL(k, i)];
+      if (a == cc) dg += v;
+      else if (a >= 0) ok &= slot_add(tc, tv, m, a, v);
+    }
+  }
+  slot_store(L, cc, tc, tv, m, dg);
+  if (!ok) d.s->mg_fail = 1;
+}
+
+// level l+1 from level l: one thread per coarse row sums its (up to) 2x2 child rows
+__global__ void k_mg_coarsen(MgLevel F, MgLevel G, Scal* s) {
+  const int C = blockIdx.x * blockDim.x + threadIdx.x;
+  if (C >= G.n) return;
+  const int X = C % G.gx, Y = C / G.gx;
+  int tc[MG_SLOTS];
+  double tv[MG_SLOTS];
+  int m = 0;
+  double dg = 0.0;
+  bool ok = true;
+  for (int q = 0; q < 4; ++q) {
+    const int fx = 2 * X + (q & 1), fy = 2 * Y + (q >> 1);
+    if (fx >= F.gx || fy >= F.gy) continue;
+    const int f = fx + fy * F.gx;
+    dg += F.diag[f];
+    const int cnt = F.cnt[f];
+    for (int t = 0; t < cnt; ++t) {
+      const int cf = F.col[(size_t)t * F.n + f];
+      const int a = (cf % F.gx) / 2 + ((cf / F.gx) / 2) * G.gx;
+      const double v = F.val[(size_t)t * F.n + f];
+      if (a == C) dg += v;
+      else ok &= slot_add(tc, tv, m, a, v);
+    }
+  }
+  slot_store(G, C, tc, tv, m, dg);
+  if (!ok) s->mg_fail = 1;
+}
+
+// ---------------------------------------------------------------- V-cycle
+struct MgArgs {
+  BiArgs b;                  // the unpreconditioned solver's arguments
+  const MgLevel* lv;         // coarse levels, finest first
+  int nl;                    // number of coarse levels (>= 1)
+  int tail;                  // first level handled by block 0 alone
+  const int *agg, *cstart, *ccnt, *ip;  // fine aggregate (cell) of each row; cell lists
+  double *z, *fr, *dinv0, *rsum;        // fine work vectors, 1/diag, row sums
+};
+
+// (A x)_c on a coarse level; x may have been written by other blocks in this launch
+__device__ __forceinline__ double lv_Ax(const MgLevel& L, const double* x, int c) {
+  double y = __ldg(L.diag + c) * x[c];
+  const int m = __ldg(L.cnt + c);
+  for (int t = 0; t < m; ++t) y = fma(__ldg(L.val + (size_t)t * L.n + c), x[__ldg(L.col + (size_t)t * L.n + c)], y);
+  return y;
+}
+
+__device__ __forceinline__ void lv_residual(const MgLevel& L, int i0, int st) {
+  for (int c = i0; c < L.n; c += st) L.r[c] = L.b[c] - lv_Ax(L, L.x, c);
+}
+
+// restriction of F's residual into G's right-hand side, and G's first sweep from zero
+__device__ __forceinline__ void lv_restrict(const MgLevel& F, const MgLevel& G, int i0, int st) {
+  for (int C = i0; C < G.n; C += st) {
+    const int X = C % G.gx, Y = C / G.gx;
+    double b = 0.0;
+    for (int q = 0; q < 4; ++q) {
+      const int fx = 2 * X + (q & 1), fy = 2 * Y + (q >> 1);
+      if (fx < F.gx && fy < F.gy) b += F.r[fx + fy * F.gx];
+    }
+    G.b[C] = b;
+    G.x[C] = MG_OMEGA * __ldg(G.dinv + C) * b;
+  }
+}
+
+__device__ __forceinline__ void lv_prolong(const MgLevel& F, const double* gsol, int ggx, int i0, int st) {
+  for (int c = i0; c < F.n; c += st) {
+    const int X = (c % F.gx) >> 1, Y = (c / F.gx) >> 1;
+    F.x[c] = fma(MG_GAMMA, gsol[X + Y * ggx], F.x[c]);
+  }
+}
+
+// one damped Jacobi sweep of x into r
+__device__ __forceinline__ void lv_smooth(const MgLevel& L, int i0, int st) {
+  for (int c = i0; c < L.n; c += st)
+    L.r[c] = fma(MG_OMEGA * __ldg(L.dinv + c), L.b[c] - lv_Ax(L, L.x, c), L.x[c]);
+}
+
+// the solution of level l after the upward pass: post-smoothed into r, or x on the coarsest
+__device__ __forceinline__ const double* lv_sol(const MgArgs& a, int l) {
+  return l == a.nl - 1 ? a.lv[l].x : a.lv[l].r;
+}
+
+// levels tail..nl-1 by block 0 alone
+__device__ void mg_block_levels(const MgArgs& a) {
+  const int i0 = threadIdx.x, st = blockDim.x;
+  for (int l = a.tail; l + 1 < a.nl; ++l) {
+    const MgLevel F = a.lv[l], G = a.lv[l + 1];
+    lv_residual(F, i0, st);
+    __syncthreads();
+    lv_restrict(F, G, i0, st);
+    __syncthreads();
+  }
+  const MgLevel K = a.lv[a.nl - 1];
+  for (int sw = 0; sw < MG_SWEEPS; ++sw) {
+    lv_smooth(K, i0, st);
+    __syncthreads();
+    for (int c = i0; c < K.n; c += st) K.x[c] = K.r[c];
+    __syncthreads();
+  }
+  for (int l = a.nl - 2; l >= a.tail; --l) {
+    const MgLevel F = a.lv[l];
+    lv_prolong(F, lv_sol(a, l + 1), a.lv[l + 1].gx, i0, st);
+    __syncthreads();
+    lv_smooth(F, i0, st);
+    __syncthreads();
+  }
+}
+
+// out = M^-1 q by one V-cycle; the last loop also writes the block partial of sum(out) into
+// slot.  q needs only its own rows complete (the calling thread wrote them).
+__device__ bool mg_vcycle(const MgArgs& a, const double* q, double* out, double* slot, double* sh, int tid,
+                          int stride) {
+  const int n = a.b.n;
+  Scal* s = a.b.sc;
+  double* z = a.z;
+  for (int i = tid; i < n; i += stride) z[i] = MG_OMEGA * a.dinv0[i] * q[i];
+  if (!grid_sync(s)) return false;
+  for (int i = tid; i < n; i += stride) a.fr[i] = q[i] - spmv_row(a.b, z, i);
+  if (!grid_sync(s)) return false;
+  {  // restriction to the cells (level 1)
+    const MgLevel L1 = a.lv[0];
+    for (int cc = tid; cc < L1.n; cc += stride) {
+      const int s0 = __ldg(a.cstart + cc), ne = __ldg(a.ccnt + cc);
+      double b = 0.0;
+      for (int k = 0; k < ne; ++k) {
+        const int i = __ldg(a.ip + s0 + k);
+        if (i >= n) break;
+        b += a.fr[i];
+      }
+      L1.b[cc] = b;
+      L1.x[cc] = MG_OMEGA * __ldg(L1.dinv + cc) * b;
+    }
+  }
+  if (!grid_sync(s)) return false;
+  for (int l = 0; l < a.tail; ++l) {
+    const MgLevel F = a.lv[l], G = a.lv[l + 1];
+    lv_residual(F, tid, stride);
+    if (!grid_sync(s)) return false;
+    lv_restrict(F, G, tid, stride);
+    if (!grid_sync(s)) return false;
+  }
+  if (blockIdx.x == 0) mg_block_levels(a);
+  if (!grid_sync(s)) return false;
+  for (int l = a.tail - 1; l >= 0; --l) {
+    const MgLevel F = a.lv[l];
+    lv_prolong(F, lv_sol(a, l + 1), a.lv[l + 1].gx, tid, stride);
+    if (!grid_sync(s)) return false;
+    lv_smooth(F, tid, stride);
+    if (!grid_sync(s)) return false;
+  }
+  {  // prolongation to the particles
+    const double* g1 = lv_sol(a, 0);
+    for (int i = tid; i < n; i += stride) {
+      const int c = __ldg(a.agg + i);
+      if (c >= 0) z[i] = fma(MG_GAMMA, g1[c], z[i]);
+    }
+  }
+  if (!grid_sync(s)) return false;
+  double acc = 0.0;
+  for (int i = tid; i < n; i += stride) {
+    const double o = fma(MG_OMEGA * a.dinv0[i], q[i] - spmv_row(a.b, z, i), z[i]);
+    out[i] = o;
+    acc += o;
+  }
+  write_partials(acc, 0.0, 1, slot, sh);
+  return true;
+}
+
+// ---------------------------------------------------------------- preconditioned BiCGSTAB
+template <bool NONULL>
+__global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
+  __shared__ double sh[64];
+  __shared__ double shv[4];
+  const BiArgs& a = m.b;
+  const int n = a.n;
+  const int nb = gridDim.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int stride = gridDim.x * blockDim.x;
+  Scal* s = a.sc;
+  if (*((volatile int*)&s->first_error)) return;  // this state already failed a step
+  const bool use_mg = *((volatile int*)&s->mg_fail) == 0;
+  double* part = a.part;
+  const double rinv1 = 1.0 / (1.0 + 1.0e-15);
+  const double small = NONULL ? 1.0e-6 : 4.0;  // open solver: the integer expression 10-6
+  double red[2];
+  double acc = 0.0;
+  // out = M^-1 q (q: own rows complete) and the block partial of sum(out) into slot
+  auto precond = [&](const double* q, double* out, double* slot) -> bool {
+    if (use_mg) return mg_vcycle(m, q, out, slot, sh, tid, stride);
+    double sum = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      const double o = NONULL ? q[i] * rinv1 : q[i] * a.rinvM[i];
+      out[i] = o;
+      sum += o;
+    }
+    write_partials(sum, 0.0, 1, slot, sh);
+    return true;
+  };
+  for (int i = tid; i < n; i += stride) {  // 1/diag and row sums of the fine matrix
+    const double dg = __ldg(a.diag + i);
+    double rs = dg;
+    const int cnt = __ldg(a.cnt + i);
+    for (int k = 0; k < cnt; ++k) rs += __ldg(a.val + (size_t)k * a.stride + i);
+    m.dinv0[i] = dg != 0.0 ? 1.0 / dg : 0.0;
+    m.rsum[i] = rs;
+    if (!NONULL) a.rinvM[i] = 1.0 / (dg + 1.0e-15);
+  }
+  if (a.warm) {  // x0 = P of the previous step
+    for (int i = tid; i < n; i += stride) {
+      double xi = a.P[i];
+      a.x[i] = xi;
+      a.pinv[i] = xi;
+    }
+    if (!grid_sync(s)) return;
+  }
+  for (int i = tid; i < n; i += stride) {
+    double bi = a.B[i];
+    if (a.warm) bi = bi - spmv_row(a, a.pinv, i);
+    else a.x[i] = 0.0;
+    a.r[i] = bi;
+    a.rb[i] = bi;
+    a.v[i] = 0.0;
+    a.p[i] = 0.0;
+    acc = fma(bi, bi, acc);
+  }
+  write_partials(acc, 0.0, 1, part + 10 * (size_t)nb, sh);
+  if (!grid_sync(s)) return;
+  reduce_partials(part + 10 * (size_t)nb, nb, 1, red, shv);
+  double rho = red[0], rho0 = 1.0, alpha = 1.0, omega = 1.0;
+  double n2r0 = 1.0, n2s0 = 1.0, resid = 0.0;
+  int iter = 1, warn = 0;
+  bool done = false;
+  while (iter <= a.itermax) {
+    if (rho == 0.0) { warn |= VEBI_WARN_BICGSTAB_BREAKDOWN; done = true; break; }
+    const double beta = rho / (rho0 + 1.0e-15) * alpha / (omega + 1.0e-15);
+    acc = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      double pi = (iter == 1) ? a.r[i] : fma(beta, fma(-omega, a.v[i], a.p[i]), a.r[i]);
+      a.p[i] = pi;
+      acc += pi;
+    }
+    if (NONULL) {
+      write_partials(acc, 0.0, 1, part, sh);
+      if (!grid_sync(s)) return;
+      reduce_partials(part, nb, 1, red, shv);
+      const double mean = red[0] / (double)n;
+      for (int i = tid; i < n; i += stride) a.p[i] = a.p[i] - mean;
+    }
+    // p_hat = M^-1 p, made mean-free (closed domains) through mp
+    if (!precond(a.p, a.pinv, part + 1 * (size_t)nb)) return;
+    if (!grid_sync(s)) return;
+    reduce_partials(part + 1 * (size_t)nb, nb, 1, red, shv);
+    const double mp = NONULL ? red[0] / (double)n : 0.0;
+    // v = A (p_hat - mp) ; (r_bar, v)
+    acc = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      double vi = fma(-mp, m.rsum[i], spmv_row(a, a.pinv, i));
+      a.v[i] = vi;
+      acc = fma(a.rb[i], vi, acc);
+    }
+    write_partials(acc, 0.0, 1, part + 2 * (size_t)nb, sh);
+    if (!grid_sync(s)) return;
+    reduce_partials(part + 2 * (size_t)nb, nb, 1, red, shv);
+    alpha = rho / (red[0] + 1.0e-15);
+    double a2 = 0.0;
+    acc = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      double si = fma(-alpha, a.v[i], a.r[i]);
+      a.s[i] = si;
+      acc = fma(si, si, acc);
+      a2 += si;
+    }
+    write_partials(acc, a2, 2, part + 4 * (size_t)nb, sh);
+    if (!grid_sync(s)) return;
+    reduce_partials(part + 4 * (size_t)nb, nb, 2, red, shv);
+    const double n2s = red[0];
+    const double mean_s = red[1] / (double)n;
+    if (iter == 1) n2s0 = (n2s <= small) ? 1.0 : n2s;
+    if (n2s <= a.tol * a.tol * n2s0) {
+      for (int i = tid; i < n; i += stride) a.x[i] = fma(alpha, a.pinv[i] - mp, a.x[i]);
+      resid = sqrt(n2s / n2s0);
+      done = true;
+      break;
+    }
+    if (NONULL)
+      for (int i = tid; i < n; i += stride) a.s[i] = a.s[i] - mean_s;
+    if (!precond(a.s, a.sinv, part + 3 * (size_t)nb)) return;
+    if (!grid_sync(s)) return;
+    reduce_partials(part + 3 * (size_t)nb, nb, 1, red, shv);
+    const double ms = NONULL ? red[0] / (double)n : 0.0;
+    // t = A (s_hat - ms) ; (t, s) ; |t|^2
+    acc = 0.0;
+    a2 = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      double ti = fma(-ms, m.rsum[i], spmv_row(a, a.sinv, i));
+      a.t[i] = ti;
+      acc = fma(ti, a.s[i], acc);
+      a2 = fma(ti, ti, a2);
+    }
+    write_partials(acc, a2, 2, part + 6 * (size_t)nb, sh);
+    if (!grid_sync(s)) return;
+    reduce_partials(part + 6 * (size_t)nb, nb, 2, red, shv);
+    omega = red[0] / (red[1] + 1.0e-15);
+    acc = 0.0;
+    a2 = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      a.x[i] = fma(omega, a.sinv[i] - ms, fma(alpha, a.pinv[i] - mp, a.x[i]));
+      double ri = fma(-omega, a.t[i], a.s[i]);
+      a.r[i] = ri;
+      acc = fma(ri, ri, acc);
+      a2 = fma(a.rb[i], ri, a2);
+    }
+    write_partials(acc, a2, 2, part + 8 * (size_t)nb, sh);
+    if (!grid_sync(s)) return;
+    reduce_partials(part + 8 * (size_t)nb, nb, 2, red, shv);
+    const double n2r = red[0];
+    if (iter == 1) n2r0 = (n2r <= small) ? 1.0 : n2r;
+    resid = sqrt(n2r / n2r0);
+    if (n2r <= a.tol * a.tol * n2r0) { done = true; break; }
+    iter = iter + 1;
+    rho0 = rho;
+    rho = red[1];
+  }
+  if (!done) warn |= VEBI_WARN_MAXITER;
+  for (int i = tid; i < n; i += stride) a.P[i] = a.x[i];
+  if (tid == 0) {
+    s->ls_iters = iter;
+    s->ls_iters_total += iter;
+    s->ls_residual = resid;
+    atomicOr(&s->warnings, warn);
+  }
+}
+
+// ---------------------------------------------------------------- host side
+int ppe_mg_blocks(int nsm) {
+  int per = 0, per2 = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_bicgstab_mg<true>, TPB, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, k_bicgstab_mg<false>, TPB, 0);
+  per = per < per2 ? per : per2;
+  if (per < 1) per = 1;
+  return per * nsm;
+}
+
+// coarse level sizes for a gx x gy cell grid: halve until at most MG_COARSEST aggregates
+std::vector<int> mg_level_dims(int gx, int gy) {
+  std::vector<int> dims;
+  for (int l = 0; l < MG_MAX_LEVELS; ++l) {
+    dims.push_back(gx);
+    dims.push_back(gy);
+    if ((long long)gx * gy <= MG_COARSEST || (gx <= 1 && gy <= 1)) break;
+    gx = (gx + 1) / 2;
+    gy = (gy + 1) / 2;
+  }
+  return dims;
+}
+
+void launch_ppe_mg(Ctx& x) {
+  const Consts& c = x.c;
+  const Dev& d = x.d;
+  const int nl = (int)x.mg.size();
+  VEBI_LAUNCH(x, k_mg_level1, grid_for(x.mg[0].n), TPB, c, d, x.mg[0]);
+  for (int l = 0; l + 1 < nl; ++l) VEBI_LAUNCH(x, k_mg_coarsen, grid_for(x.mg[l + 1].n), TPB, x.mg[l], x.mg[l + 1], d.s);
+  int tail = nl - 1;
+  for (int l = 0; l < nl; ++l)
+    if (x.mg[l].n <= MG_BLOCK_ROWS) { tail = l; break; }
+  int nblk = x.mg_blocks;
+  const long long rows_per_block = (long long)TPB * (x.solver_rows_per_thread > 0 ? x.solver_rows_per_thread : 1);
+  long long need = (c.npfb + rows_per_block - 1) / rows_per_block;
+  if (need < nblk) nblk = (int)(need < 1 ? 1 : need);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nblk);
+  cfg.blockDim = dim3(TPB);
+  cfg.stream = x.st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  MgArgs m{BiArgs{d.bx, d.br, d.brb, d.bv, d.bp, d.bpi, d.bs, d.bsi, d.bt, d.bM, d.partials, d.p, d.ppe_B,
+                  d.ppe_diag, d.ppe_val, d.ppe_col, d.ij_count, d.s, (long long)c.npfb, c.npfb, c.itermax, c.tol,
+                  c.warm_start},
+           x.d_mg, nl, tail, d.cellpart, d.cell_start, d.cell_cnt, d.ip, x.mg_z, x.mg_fr, x.mg_dinv0, x.mg_rsum};
+  if (c.open_domain == 0) cudaLaunchKernelEx(&cfg, k_bicgstab_mg<true>, m);
+  else cudaLaunchKernelEx(&cfg, k_bicgstab_mg<false>, m);
+  x.launches++;
+}
+
+}  // namespace vebi

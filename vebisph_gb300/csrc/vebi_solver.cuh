@@ -1,0 +1,118 @@
+// vebi_solver.cuh -- building blocks of the persistent cooperative PPE solvers: the bounded
+// grid barrier, the deterministic block-partial reductions, the solver arguments and the
+// FP64 ELL row product (sparse_atime, linear_solver.F90:254-273).
+#pragma once
+#include "vebi_ctx.cuh"
+
+namespace vebi {
+
+constexpr unsigned long long SPIN_LIMIT = 1ull << 25;  // ~2-4 s of __nanosleep(64) polls
+
+// bounded grid-wide barrier for a co-resident (cooperative) grid; false on error/timeout
+__device__ __forceinline__ bool grid_sync(Scal* s) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* vgen = &s->bar_gen;
+    volatile int* verr = &s->error;
+    unsigned int g = *vgen;
+    __threadfence();
+    unsigned int arrived = atomicAdd((unsigned int*)&s->bar_count, 1u) + 1u;
+    if (arrived == gridDim.x) {
+      atomicExch((unsigned int*)&s->bar_count, 0u);
+      __threadfence();
+      atomicAdd((unsigned int*)&s->bar_gen, 1u);
+    } else {
+      unsigned long long spins = 0;
+      while (*vgen == g) {
+        if (*verr != 0) break;
+        if (++spins > SPIN_LIMIT) {
+          atomicCAS((int*)&s->error, 0, VEBI_ERR_TIMEOUT);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *((volatile int*)&s->error) == 0;
+}
+
+// sum of the block partials of `slot` in a fixed order; identical in every block
+__device__ __forceinline__ void reduce_partials(const double* part, int nb, int nval, double* out,
+                                                double* shv) {
+  if (threadIdx.x < 32) {
+    for (int q = 0; q < nval; ++q) {
+      double v = 0.0;
+      for (int b = threadIdx.x; b < nb; b += 32) v += __ldcg(part + (size_t)q * nb + b);
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (threadIdx.x == 0) shv[q] = v;
+    }
+  }
+  __syncthreads();
+  for (int q = 0; q < nval; ++q) out[q] = shv[q];
+  __syncthreads();
+}
+
+// block partial of one or two values into part[q*nb + blockIdx.x]
+__device__ __forceinline__ void write_partials(double a, double b, int nval, double* part, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) { sh[w] = a; sh[32 + w] = b; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sa = 0.0, sb = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { sa += sh[q]; sb += sh[32 + q]; }
+    part[blockIdx.x] = sa;
+    if (nval > 1) part[gridDim.x + blockIdx.x] = sb;
+  }
+  __syncthreads();
+}
+
+// Solver arguments: only what the loop touches (keeps the kernel's register footprint small).
+struct BiArgs {
+  double *x, *r, *rb, *v, *p, *pinv, *s, *sinv, *t, *rinvM, *part, *P;
+  const double *B, *diag, *val;
+  const int *col, *cnt;
+  Scal* sc;
+  long long stride;
+  int n, itermax;
+  double tol;
+  int warm;
+};
+
+// y_i = A_ii x_i + sum_k A_ik x_col(ik)  (sparse_atime, linear_solver.F90:254-273).  Four
+// interleaved accumulators keep four independent load chains (column -> x) in flight per thread.
+// x was written inside this kernel by other blocks: the grid barrier's release/acquire fences
+// (gpu scope, followed by a CTA barrier) make those writes visible to the L1-cached loads
+// (ld.global.ca) that follow, as in a cooperative-groups grid sync; neighbouring rows share most
+// of their columns, so the gathers mostly hit L1.
+__device__ __forceinline__ double spmv_row(const BiArgs& a, const double* xv, int i) {
+  const int cnt = __ldg(a.cnt + i);
+  const double* vp = a.val + i;
+  const int* cp = a.col + i;
+  const long long st = a.stride;
+  double b0 = __ldg(a.diag + i) * __ldca(xv + i), b1 = 0.0, b2 = 0.0, b3 = 0.0;
+  int k = 0;
+  for (; k + 3 < cnt; k += 4) {
+    const int c0 = __ldg(cp), c1 = __ldg(cp + st), c2 = __ldg(cp + 2 * st), c3 = __ldg(cp + 3 * st);
+    const double v0 = __ldg(vp), v1 = __ldg(vp + st), v2 = __ldg(vp + 2 * st), v3 = __ldg(vp + 3 * st);
+    b0 = fma(v0, __ldca(xv + c0), b0);
+    b1 = fma(v1, __ldca(xv + c1), b1);
+    b2 = fma(v2, __ldca(xv + c2), b2);
+    b3 = fma(v3, __ldca(xv + c3), b3);
+    cp += 4 * st;
+    vp += 4 * st;
+  }
+  for (; k < cnt; ++k) {
+    b0 = fma(__ldg(vp), __ldca(xv + __ldg(cp)), b0);
+    cp += st;
+    vp += st;
+  }
+  return (b0 + b1) + (b2 + b3);
+}
+
+}  // namespace vebi
