@@ -153,6 +153,19 @@ def ppe_bytes_per_iteration(n_rows: int, nnz_off: int, mixed: bool = False) -> f
     return 2.0 * (12.0 * nnz_off + 44.0 * n_rows) + 168.0 * n_rows
 
 
+def mg_bytes_per_iteration(n_rows: int, nnz_off: int, n_cells: int, mixed: bool = False) -> float:
+    """Algorithmic bytes of one multigrid-preconditioned BiCGSTAB iteration (closed domain): the
+    unpreconditioned iteration, plus 16 B per row for the mean corrections (row sums), plus two
+    V-cycles.  Particle level of a V-cycle (pre-smoothing only): FP64 12 B per slot + 100 B per
+    row (first sweep 24, residual product 44, restriction 12, prolongation and output 20); mixed
+    8 B per slot + 72 B per row (16, 32, 8, 16).  Coarse levels: ~390 B per cell (the cell
+    level's ELL rows read by the residual and the smoothing sweep, work vectors, and the
+    geometric sum of the coarser levels)."""
+    outer = ppe_bytes_per_iteration(n_rows, nnz_off, mixed) + 16.0 * n_rows
+    fine = (8.0 * nnz_off + 72.0 * n_rows) if mixed else (12.0 * nnz_off + 100.0 * n_rows)
+    return outer + 2.0 * (fine + 390.0 * n_cells)
+
+
 def cpu_baseline(case, gpu_iters_per_step: float, itermax_sample: int):
     """Time the oracle (CPU restatement of the reference) on this host's cores on a bounded
     sample: one full step whose BiCGSTAB is capped at itermax_sample iterations; the step time
@@ -209,7 +222,13 @@ def run_gb300(args, dist: Dist):
     # roofline of the dominant kernel: the persistent BiCGSTAB launch (one per step)
     cnt = sol.get("ij_count")
     nnz_off = int(cnt.sum())
-    bytes_iter = ppe_bytes_per_iteration(case.npfb, nnz_off, mixed=prec == abi.PREC_MIXED)
+    mg = case.ppe_precond == abi.PRECOND_MULTIGRID
+    if mg:
+        cp = sol.get("cellpart")[: case.npfb]
+        n_cells = int(np.unique(cp[cp >= 0]).size)
+        bytes_iter = mg_bytes_per_iteration(case.npfb, nnz_off, n_cells, mixed=prec == abi.PREC_MIXED)
+    else:
+        bytes_iter = ppe_bytes_per_iteration(case.npfb, nnz_off, mixed=prec == abi.PREC_MIXED)
     per_launch_bytes = bytes_iter * iters_per_step
     per_launch_s = solve_ms * 1e-3 / args.steps
     achieved = per_launch_bytes / per_launch_s / 1e9
@@ -222,7 +241,10 @@ def run_gb300(args, dist: Dist):
         traffic = tj["dram_bytes_per_row_iteration"] * case.npfb * iters_per_step
     kname = ("k_bicgstab_mixed<true> (persistent cooperative BiCGSTAB, FP32 SpMV, one launch per step)"
              if prec == abi.PREC_MIXED else "k_bicgstab<true> (persistent cooperative BiCGSTAB, one launch per step)")
-    if prec == abi.PREC_MIXED:
+    if mg:
+        kname = ("k_bicgstab_mixed_mg<true>" if prec == abi.PREC_MIXED else "k_bicgstab_mg<true>") + \
+            " (persistent cooperative BiCGSTAB with the multigrid V-cycle; the set-up kernels are in the stage time)"
+    if prec == abi.PREC_MIXED or mg:
         traffic = None
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
@@ -429,6 +451,23 @@ def mixed_summary(f64: dict, mx: dict) -> dict:
                      "(tests/test_gpu_mixed.py)")}
 
 
+def multigrid_summary(plain: dict, f64: dict, mx: dict) -> dict:
+    """The opt-in multigrid-preconditioned PPE on the same workload: FP64 and mixed precision,
+    both converging to the solver tolerance; speed-ups and the mixed-vs-FP64 differences."""
+    keep = ("value", "ms_per_step", "LS_iters_per_step", "LS_residual_last", "stage_ms_per_step", "roofline",
+            "gpu_launches", "drag")
+    out = {"fp64": {k: f64[k] for k in keep}, "mixed": {k: mx[k] for k in keep}}
+    out["speedup_mixed_vs_fp64"] = mx["value"] / f64["value"]
+    out["speedup_fp64_vs_plain_fp64"] = f64["value"] / plain["value"]
+    out["speedup_mixed_vs_plain_fp64"] = mx["value"] / plain["value"]
+    d = mixed_summary(f64, mx)
+    out["mixed_vs_fp64"] = {"rel_diff": d["rel_diff_vs_fp64"], "drag_rel_diff": d["drag_rel_diff_vs_fp64"],
+                            "N1_wake_max": d["N1_wake_max"]}
+    out["note"] = ("opt-in (ppe_precond = VEBI_PRECOND_MULTIGRID): aggregation multigrid on the cell grid; "
+                   "both precisions converge to tol 1e-8 each step, the plain solver stops at its 1000-iteration cap")
+    return out
+
+
 def run_reference(args, dist: Dist):
     """The reference's own CPU path timed on this host: the oracle restatement (the Fortran
     reference has no compiler here), all host threads, each step a bounded sample."""
@@ -486,6 +525,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision comparison run")
+    ap.add_argument("--no-multigrid", action="store_true", help="skip the multigrid-preconditioned runs")
     ap.add_argument("--batch", type=int, default=0,
                     help="run the batched parameter sweep of this many instances instead")
     ap.add_argument("--batch-precision", choices=["fp64", "mixed"], default="mixed")
@@ -521,6 +561,13 @@ def main():
             margs.no_cpu = True
             mres = run_gb300(margs, dist)
             res["mixed"] = mixed_summary(res, mres)
+        if args.precond == "none" and not args.no_multigrid and not args.batch:
+            runs = []
+            for p in ("fp64", "mixed"):
+                gargs = argparse.Namespace(**vars(args))
+                gargs.precision, gargs.precond, gargs.no_e2e, gargs.no_cpu = p, "multigrid", True, True
+                runs.append(run_gb300(gargs, dist))
+            res["multigrid"] = multigrid_summary(res, runs[0], runs[1])
         res.pop("_fields", None)
     else:
         from oracle import build as ob

@@ -64,3 +64,23 @@ def test_multigrid_is_deterministic(libs):
         s.close()
     assert out[0][0] == out[1][0]
     assert np.array_equal(out[0][1], out[1][1]) and np.array_equal(out[0][2], out[1][2])
+
+
+@pytest.mark.parametrize("name", ["poiseuille40", "cylinder20k", "free_surface_open"])
+def test_mixed_multigrid_close_to_fp64(libs, name):
+    """Mixed precision with the preconditioner against the FP64 step with it: velocity, and for
+    the cylinder the drag, within 1e-4 after three steps (both solves converge)."""
+    StepSolver, _ = libs
+    a = StepSolver(_mg(CASES[name]()), precision=abi.PREC_FP64)
+    b = StepSolver(_mg(CASES[name]()), precision=abi.PREC_MIXED)
+    n = a.case.npfb
+    for _ in range(3):
+        sa, sb = a.step(), b.step()
+        assert sb["error"] == 0 and not (sb["warnings"] & abi.WARN_MAXITER)
+    us = max(np.abs(a.get("ux")[:n]).max(), np.abs(a.get("uy")[:n]).max())
+    for nm in ("ux", "uy"):
+        assert relerr(b.get(nm)[:n], a.get(nm)[:n], us) <= 1e-4, nm
+    if a.case.nb_circles:
+        assert abs(sb["circle_force"][0] - sa["circle_force"][0]) <= 1e-4 * abs(sa["circle_force"][0])
+    a.close()
+    b.close()

@@ -252,6 +252,7 @@ static int allocate_all(Ctx& x) {
     A_(x.d_mg, x.mg.size());
     cudaMemcpy(x.d_mg, x.mg.data(), sizeof(MgLevel) * x.mg.size(), cudaMemcpyHostToDevice);
     A_(x.mg_z, n); A_(x.mg_fr, n); A_(x.mg_dinv0, n); A_(x.mg_rsum, n);
+    A_(x.mg_ragg, n * MG_ROW_SLOTS); A_(x.mg_rval, n * MG_ROW_SLOTS); A_(x.mg_rcnt, n);
   }
 #undef A_
   return VEBI_OK;

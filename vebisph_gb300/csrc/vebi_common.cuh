@@ -78,11 +78,12 @@ struct Scal {
 // multigrid preconditioner (opt-in): coarse-row capacity, coarsest size, level cap, levels run
 // by one block, coarsest sweeps, Jacobi damping, coarse-correction scaling
 constexpr int MG_SLOTS = 24;
-constexpr int MG_COARSEST = 2048;
+constexpr int MG_ROW_SLOTS = 16;
+constexpr int MG_COARSEST = 32;
 constexpr int MG_MAX_LEVELS = 12;
 constexpr int MG_BLOCK_ROWS = 8192;
-constexpr int MG_SWEEPS = 8;
-constexpr double MG_OMEGA = 0.8;
+constexpr int MG_SWEEPS = 16;
+constexpr double MG_OMEGA = 0.9;
 constexpr double MG_GAMMA = 1.8;
 
 // One coarse level of the multigrid preconditioner: the cell grid (level 1) or a 2x2

@@ -40,6 +40,8 @@ struct Ctx {
   MgLevel* d_mg = nullptr;         // device copy of the level descriptors
   int mg_blocks = 0;               // co-resident blocks of the preconditioned solver
   double *mg_z = nullptr, *mg_fr = nullptr, *mg_dinv0 = nullptr, *mg_rsum = nullptr;
+  int *mg_ragg = nullptr, *mg_rcnt = nullptr;  // per-row (cell, value) pairs of the level-1 build
+  double* mg_rval = nullptr;
   std::vector<void*> allocs;
   vebi_step_stats last{};
 };

@@ -13,8 +13,10 @@
 //
 // V-cycle, one per preconditioning step: one damped Jacobi sweep (MG_OMEGA) from zero, the
 // residual, restriction (the sum over each aggregate), the coarser levels, prolongation scaled
-// by MG_GAMMA (over-correction for piecewise-constant interpolation), one post-smoothing sweep.
-// The coarsest level takes MG_SWEEPS Jacobi sweeps.  Levels of at most MG_BLOCK_ROWS rows run in
+// by MG_GAMMA (over-correction for piecewise-constant interpolation) and, on the coarse levels,
+// one post-smoothing sweep; the particle level is pre-smoothed only (two particle-level
+// products per V-cycle cost more than the iterations they save).  The coarsest level takes
+// MG_SWEEPS Jacobi sweeps.  Levels of at most MG_BLOCK_ROWS rows run in
 // block 0 alone with block barriers.  Every sum runs in a fixed order.
 //
 // Solver.  BiCGSTAB with right preconditioning, in the persistent cooperative kernel of the
@@ -29,12 +31,13 @@ namespace vebi {
 #define ELL(k, i) ((size_t)(k) * c.npfb + (i))
 
 // ---------------------------------------------------------------- set-up (every step)
-// add v to column `col` of a row's slot table; false when the table is full
+// add v to column `col` of a row's slot table of capacity CAP; false when the table is full
+template <int CAP = MG_SLOTS>
 __device__ __forceinline__ bool slot_add(int* tc, double* tv, int& m, int col, double v) {
   int t = 0;
   while (t < m && tc[t] != col) ++t;
   if (t == m) {
-    if (m == MG_SLOTS) return false;
+    if (m == CAP) return false;
     tc[m] = col;
     tv[m] = 0.0;
     ++m;
@@ -54,8 +57,41 @@ __device__ __forceinline__ void slot_store(const MgLevel& L, int row, const int*
   L.dinv[row] = dg != 0.0 ? 1.0 / dg : 0.0;
 }
 
-// level 1: one thread per cell sums the PPE rows of the cell's particles (ascending index)
-__global__ void k_mg_level1(Consts c, Dev d, MgLevel L) {
+// Level 1 in two passes.  Rows: one thread per PPE row sums the row by the cell of each
+// column (its own cell first, with the diagonal) into MG_ROW_SLOTS (cell, value) pairs,
+// [t][i] layout.  Cells: one thread per cell merges its particles' pairs in ascending particle
+// order.  val32 (mixed precision) replaces the FP64 values when given.
+__global__ void k_mg_rows(Consts c, Dev d, const float* __restrict__ val32, int* __restrict__ ragg,
+                          double* __restrict__ rval, int* __restrict__ rcnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.npfb) return;
+  const int own = d.cellpart[i];
+  if (own < 0) {  // a binned particle belongs to no cell
+    rcnt[i] = 0;
+    return;
+  }
+  int tc[MG_ROW_SLOTS];
+  double tv[MG_ROW_SLOTS];
+  tc[0] = own;
+  tv[0] = d.ppe_diag[i];
+  int m = 1;
+  bool ok = true;
+  const int cnt = d.ij_count[i];
+  for (int k = 0; k < cnt; ++k) {
+    const int a = d.cellpart[d.ppe_col[ELL(k, i)]];
+    const double v = val32 ? (double)val32[ELL(k, i)] : d.ppe_val[ELL(k, i)];
+    if (a >= 0) ok &= slot_add<MG_ROW_SLOTS>(tc, tv, m, a, v);
+  }
+  for (int t = 0; t < m; ++t) {
+    ragg[(size_t)t * c.npfb + i] = tc[t];
+    rval[(size_t)t * c.npfb + i] = tv[t];
+  }
+  rcnt[i] = m;
+  if (!ok) d.s->mg_fail = 1;
+}
+
+__global__ void k_mg_level1(Consts c, Dev d, MgLevel L, const int* __restrict__ ragg,
+                            const double* __restrict__ rval, const int* __restrict__ rcnt) {
   const int cc = blockIdx.x * blockDim.x + threadIdx.x;
   if (cc >= L.n) return;
   int tc[MG_SLOTS];
@@ -67,13 +103,12 @@ __global__ void k_mg_level1(Consts c, Dev d, MgLevel L) {
   for (int q = 0; q < ne; ++q) {
     const int i = d.ip[s0 + q];
     if (i >= c.npfb) break;  // mirrors follow the particles in a sorted cell list
-    dg += d.ppe_diag[i];
-    const int cnt = d.ij_count[i];
-    for (int k = 0; k < cnt; ++k) {
-      const int a = d.cellpart[d.ppe_col[ELL(k, i)]];
-      const double v = d.ppe_val[ELL(k, i)];
+    const int mi = rcnt[i];
+    for (int t = 0; t < mi; ++t) {
+      const int a = ragg[(size_t)t * c.npfb + i];
+      const double v = rval[(size_t)t * c.npfb + i];
       if (a == cc) dg += v;
-      else if (a >= 0) ok &= slot_add(tc, tv, m, a, v);
+      else ok &= slot_add(tc, tv, m, a, v);
     }
   }
   slot_store(L, cc, tc, tv, m, dg);
@@ -230,17 +265,12 @@ __device__ bool mg_vcycle(const MgArgs& a, const double* q, double* out, double*
     lv_smooth(F, tid, stride);
     if (!grid_sync(s)) return false;
   }
-  {  // prolongation to the particles
-    const double* g1 = lv_sol(a, 0);
-    for (int i = tid; i < n; i += stride) {
-      const int c = __ldg(a.agg + i);
-      if (c >= 0) z[i] = fma(MG_GAMMA, g1[c], z[i]);
-    }
-  }
-  if (!grid_sync(s)) return false;
+  // prolongation to the particles (the particle level is pre-smoothed only)
+  const double* g1 = lv_sol(a, 0);
   double acc = 0.0;
   for (int i = tid; i < n; i += stride) {
-    const double o = fma(MG_OMEGA * a.dinv0[i], q[i] - spmv_row(a.b, z, i), z[i]);
+    const int c = __ldg(a.agg + i);
+    const double o = c >= 0 ? fma(MG_GAMMA, g1[c], z[i]) : z[i];
     out[i] = o;
     acc += o;
   }
@@ -413,12 +443,272 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
   }
 }
 
+// ---------------------------------------------------------------- mixed precision
+// The mixed-precision solver (FP64 recurrences, FP32 difference-form SpMV) with the same
+// V-cycle, whose particle level runs in FP32: the smoothing vector and the fine residual are
+// FP32 and the fine products use the FP32 values in difference form.  The coarse levels are the
+// FP64 ones of the FP64 solver.  The preconditioner need not be exact: its rounding changes the
+// iteration count, not the residual test the solve stops on.
+struct MgMxArgs {
+  MxArgs b;
+  const MgLevel* lv;
+  int nl, tail;
+  const int *agg, *cstart, *ccnt, *ip;
+  float *z, *fr, *dinv0;
+};
+
+// sum_k A_ik (z_col - z_i) + rowsum_i z_i in FP32 (one FP32 vector)
+__device__ __forceinline__ float spmv_diff32s(const MxArgs& a, const float* z, int i) {
+  const int cnt = __ldg(a.cnt + i);
+  const float* vp = a.val32 + i;
+  const int* cp = a.col + i;
+  const long long st = a.stride;
+  const float zi = __ldca(z + i);
+  float b0 = 0.f, b1 = 0.f, b2 = 0.f, b3 = 0.f;
+  int k = 0;
+  for (; k + 3 < cnt; k += 4) {
+    const int c0 = __ldg(cp), c1 = __ldg(cp + st), c2 = __ldg(cp + 2 * st), c3 = __ldg(cp + 3 * st);
+    const float v0 = __ldg(vp), v1 = __ldg(vp + st), v2 = __ldg(vp + 2 * st), v3 = __ldg(vp + 3 * st);
+    b0 = fmaf(v0, __ldca(z + c0) - zi, b0);
+    b1 = fmaf(v1, __ldca(z + c1) - zi, b1);
+    b2 = fmaf(v2, __ldca(z + c2) - zi, b2);
+    b3 = fmaf(v3, __ldca(z + c3) - zi, b3);
+    cp += 4 * st;
+    vp += 4 * st;
+  }
+  for (; k < cnt; ++k) {
+    b0 = fmaf(__ldg(vp), __ldca(z + __ldg(cp)) - zi, b0);
+    cp += st;
+    vp += st;
+  }
+  return fmaf((float)__ldg(a.rs + i), zi, (b0 + b1) + (b2 + b3));
+}
+
+// out = M^-1 q as FP32 (hi, lo) pairs; block partial of sum(out) into slot
+__device__ bool mg_vcycle_mixed(const MgMxArgs& a, const double* q, float2* out, double* slot, double* sh,
+                                int tid, int stride) {
+  const int n = a.b.n;
+  Scal* s = a.b.sc;
+  float* z = a.z;
+  for (int i = tid; i < n; i += stride) z[i] = (float)MG_OMEGA * a.dinv0[i] * (float)q[i];
+  if (!grid_sync(s)) return false;
+  for (int i = tid; i < n; i += stride) a.fr[i] = (float)q[i] - spmv_diff32s(a.b, z, i);
+  if (!grid_sync(s)) return false;
+  {
+    const MgLevel L1 = a.lv[0];
+    for (int cc = tid; cc < L1.n; cc += stride) {
+      const int s0 = __ldg(a.cstart + cc), ne = __ldg(a.ccnt + cc);
+      double b = 0.0;
+      for (int k = 0; k < ne; ++k) {
+        const int i = __ldg(a.ip + s0 + k);
+        if (i >= n) break;
+        b += (double)a.fr[i];
+      }
+      L1.b[cc] = b;
+      L1.x[cc] = MG_OMEGA * __ldg(L1.dinv + cc) * b;
+    }
+  }
+  if (!grid_sync(s)) return false;
+  MgArgs c{};  // the coarse-level view shared with the FP64 V-cycle
+  c.lv = a.lv;
+  c.nl = a.nl;
+  c.tail = a.tail;
+  for (int l = 0; l < a.tail; ++l) {
+    const MgLevel F = a.lv[l], G = a.lv[l + 1];
+    lv_residual(F, tid, stride);
+    if (!grid_sync(s)) return false;
+    lv_restrict(F, G, tid, stride);
+    if (!grid_sync(s)) return false;
+  }
+  if (blockIdx.x == 0) mg_block_levels(c);
+  if (!grid_sync(s)) return false;
+  for (int l = a.tail - 1; l >= 0; --l) {
+    const MgLevel F = a.lv[l];
+    lv_prolong(F, lv_sol(c, l + 1), a.lv[l + 1].gx, tid, stride);
+    if (!grid_sync(s)) return false;
+    lv_smooth(F, tid, stride);
+    if (!grid_sync(s)) return false;
+  }
+  // prolongation to the particles (pre-smoothed only), output as FP32 (hi, lo) pairs
+  const double* g1 = lv_sol(c, 0);
+  double acc = 0.0;
+  for (int i = tid; i < n; i += stride) {
+    const int cc = __ldg(a.agg + i);
+    const double o = cc >= 0 ? fma(MG_GAMMA, g1[cc], (double)z[i]) : (double)z[i];
+    out[i] = split2(o);
+    acc += o;
+  }
+  write_partials(acc, 0.0, 1, slot, sh);
+  return true;
+}
+
+template <bool NONULL>
+__global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
+  __shared__ double sh[64];
+  __shared__ double shv[4];
+  const MxArgs& a = m.b;
+  const int n = a.n;
+  const int nb = gridDim.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int stride = gridDim.x * blockDim.x;
+  Scal* s = a.sc;
+  if (*((volatile int*)&s->first_error)) return;  // this state already failed a step
+  const bool use_mg = *((volatile int*)&s->mg_fail) == 0;
+  double* part = a.part;
+  const double rinv1 = 1.0 / (1.0 + 1.0e-15);
+  const double small = NONULL ? 1.0e-6 : 4.0;
+  double red[2];
+  double acc = 0.0;
+  auto precond = [&](const double* q, float2* out, double* slot) -> bool {
+    if (use_mg) return mg_vcycle_mixed(m, q, out, slot, sh, tid, stride);
+    double sum = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      const double o = NONULL ? q[i] * rinv1 : q[i] * a.rinvM[i];
+      out[i] = split2(o);
+      sum += o;
+    }
+    write_partials(sum, 0.0, 1, slot, sh);
+    return true;
+  };
+  for (int i = tid; i < n; i += stride) {
+    // 1/diag from the row sum and the FP32 off-diagonal values (diag = rowsum - sum_k A_ik)
+    double dg = __ldg(a.rs + i);
+    const int cnt = __ldg(a.cnt + i);
+    for (int k = 0; k < cnt; ++k) dg -= (double)__ldg(a.val32 + (size_t)k * a.stride + i);
+    m.dinv0[i] = dg != 0.0 ? (float)(1.0 / dg) : 0.f;
+  }
+  if (a.warm) {
+    for (int i = tid; i < n; i += stride) {
+      double xi = a.P[i];
+      a.x[i] = xi;
+      a.pi[i] = split2(xi);
+    }
+    if (!grid_sync(s)) return;
+  }
+  for (int i = tid; i < n; i += stride) {
+    double bi = a.B[i];
+    if (a.warm) bi = bi - spmv_diff32(a, a.pi, i);
+    else a.x[i] = 0.0;
+    a.r[i] = bi;
+    a.rb[i] = bi;
+    a.v[i] = 0.0;
+    a.p[i] = 0.0;
+    acc = fma(bi, bi, acc);
+  }
+  write_partials(acc, 0.0, 1, part + 10 * (size_t)nb, sh);
+  if (!grid_sync(s)) return;
+  reduce_partials(part + 10 * (size_t)nb, nb, 1, red, shv);
+  double rho = red[0], rho0 = 1.0, alpha = 1.0, omega = 1.0;
+  double n2r0 = 1.0, n2s0 = 1.0, resid = 0.0;
+  int iter = 1, warn = 0;
+  bool done = false;
+  while (iter <= a.itermax) {
+    if (rho == 0.0) { warn |= VEBI_WARN_BICGSTAB_BREAKDOWN; done = true; break; }
+    const double beta = rho / (rho0 + 1.0e-15) * alpha / (omega + 1.0e-15);
+    acc = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      double pi = (iter == 1) ? a.r[i] : fma(beta, fma(-omega, a.v[i], a.p[i]), a.r[i]);
+      a.p[i] = pi;
+      acc += pi;
+    }
+    if (NONULL) {
+      write_partials(acc, 0.0, 1, part, sh);
+      if (!grid_sync(s)) return;
+      reduce_partials(part, nb, 1, red, shv);
+      const double mean = red[0] / (double)n;
+      for (int i = tid; i < n; i += stride) a.p[i] = a.p[i] - mean;
+    }
+    if (!precond(a.p, a.pi, part + 1 * (size_t)nb)) return;
+    if (!grid_sync(s)) return;
+    reduce_partials(part + 1 * (size_t)nb, nb, 1, red, shv);
+    const double mp = NONULL ? red[0] / (double)n : 0.0;
+    acc = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      double vi = fma(-mp, __ldg(a.rs + i), spmv_diff32(a, a.pi, i));
+      a.v[i] = vi;
+      acc = fma(a.rb[i], vi, acc);
+    }
+    write_partials(acc, 0.0, 1, part + 2 * (size_t)nb, sh);
+    if (!grid_sync(s)) return;
+    reduce_partials(part + 2 * (size_t)nb, nb, 1, red, shv);
+    alpha = rho / (red[0] + 1.0e-15);
+    double a2 = 0.0;
+    acc = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      double si = fma(-alpha, a.v[i], a.r[i]);
+      a.s[i] = si;
+      acc = fma(si, si, acc);
+      a2 += si;
+    }
+    write_partials(acc, a2, 2, part + 4 * (size_t)nb, sh);
+    if (!grid_sync(s)) return;
+    reduce_partials(part + 4 * (size_t)nb, nb, 2, red, shv);
+    const double n2s = red[0];
+    const double mean_s = red[1] / (double)n;
+    if (iter == 1) n2s0 = (n2s <= small) ? 1.0 : n2s;
+    if (n2s <= a.tol * a.tol * n2s0) {
+      for (int i = tid; i < n; i += stride) a.x[i] = fma(alpha, join2(a.pi[i]) - mp, a.x[i]);
+      resid = sqrt(n2s / n2s0);
+      done = true;
+      break;
+    }
+    if (NONULL)
+      for (int i = tid; i < n; i += stride) a.s[i] = a.s[i] - mean_s;
+    if (!precond(a.s, a.si, part + 3 * (size_t)nb)) return;
+    if (!grid_sync(s)) return;
+    reduce_partials(part + 3 * (size_t)nb, nb, 1, red, shv);
+    const double ms = NONULL ? red[0] / (double)n : 0.0;
+    acc = 0.0;
+    a2 = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      double ti = fma(-ms, __ldg(a.rs + i), spmv_diff32(a, a.si, i));
+      a.t[i] = ti;
+      acc = fma(ti, a.s[i], acc);
+      a2 = fma(ti, ti, a2);
+    }
+    write_partials(acc, a2, 2, part + 6 * (size_t)nb, sh);
+    if (!grid_sync(s)) return;
+    reduce_partials(part + 6 * (size_t)nb, nb, 2, red, shv);
+    omega = red[0] / (red[1] + 1.0e-15);
+    acc = 0.0;
+    a2 = 0.0;
+    for (int i = tid; i < n; i += stride) {
+      a.x[i] = fma(omega, join2(a.si[i]) - ms, fma(alpha, join2(a.pi[i]) - mp, a.x[i]));
+      double ri = fma(-omega, a.t[i], a.s[i]);
+      a.r[i] = ri;
+      acc = fma(ri, ri, acc);
+      a2 = fma(a.rb[i], ri, a2);
+    }
+    write_partials(acc, a2, 2, part + 8 * (size_t)nb, sh);
+    if (!grid_sync(s)) return;
+    reduce_partials(part + 8 * (size_t)nb, nb, 2, red, shv);
+    const double n2r = red[0];
+    if (iter == 1) n2r0 = (n2r <= small) ? 1.0 : n2r;
+    resid = sqrt(n2r / n2r0);
+    if (n2r <= a.tol * a.tol * n2r0) { done = true; break; }
+    iter = iter + 1;
+    rho0 = rho;
+    rho = red[1];
+  }
+  if (!done) warn |= VEBI_WARN_MAXITER;
+  for (int i = tid; i < n; i += stride) a.P[i] = a.x[i];
+  if (tid == 0) {
+    s->ls_iters = iter;
+    s->ls_iters_total += iter;
+    s->ls_residual = resid;
+    atomicOr(&s->warnings, warn);
+  }
+}
+
 // ---------------------------------------------------------------- host side
 int ppe_mg_blocks(int nsm) {
-  int per = 0, per2 = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_bicgstab_mg<true>, TPB, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, k_bicgstab_mg<false>, TPB, 0);
-  per = per < per2 ? per : per2;
+  int per = 1 << 20;
+  int o[4] = {0, 0, 0, 0};
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o[0], k_bicgstab_mg<true>, TPB, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o[1], k_bicgstab_mg<false>, TPB, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o[2], k_bicgstab_mixed_mg<true>, TPB, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o[3], k_bicgstab_mixed_mg<false>, TPB, 0);
+  for (int q = 0; q < 4; ++q) per = o[q] < per ? o[q] : per;
   if (per < 1) per = 1;
   return per * nsm;
 }
@@ -436,15 +726,53 @@ std::vector<int> mg_level_dims(int gx, int gy) {
   return dims;
 }
 
+// the coarse matrices of this step, and the first level small enough for one block
+static int mg_setup(Ctx& x) {
+  const Consts& c = x.c;
+  const int nl = (int)x.mg.size();
+  const float* v32 = x.precision == VEBI_PREC_MIXED ? x.d.ppe_val32 : nullptr;
+  VEBI_LAUNCH(x, k_mg_rows, grid_for(c.npfb), TPB, c, x.d, v32, x.mg_ragg, x.mg_rval, x.mg_rcnt);
+  VEBI_LAUNCH(x, k_mg_level1, grid_for(x.mg[0].n), TPB, c, x.d, x.mg[0], x.mg_ragg, x.mg_rval, x.mg_rcnt);
+  for (int l = 0; l + 1 < nl; ++l)
+    VEBI_LAUNCH(x, k_mg_coarsen, grid_for(x.mg[l + 1].n), TPB, x.mg[l], x.mg[l + 1], x.d.s);
+  int tail = nl - 1;
+  for (int l = 0; l < nl; ++l)
+    if (x.mg[l].n <= MG_BLOCK_ROWS) { tail = l; break; }
+  return tail;
+}
+
+void launch_ppe_mg_mixed(Ctx& x) {
+  const Consts& c = x.c;
+  const Dev& d = x.d;
+  const int tail = mg_setup(x);
+  int nblk = x.mg_blocks;
+  const long long rows_per_block = (long long)TPB * (x.solver_rows_per_thread > 0 ? x.solver_rows_per_thread : 1);
+  long long need = (c.npfb + rows_per_block - 1) / rows_per_block;
+  if (need < nblk) nblk = (int)(need < 1 ? 1 : need);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nblk);
+  cfg.blockDim = dim3(TPB);
+  cfg.stream = x.st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  MgMxArgs m{MxArgs{d.bx, d.br, d.brb, d.bv, d.bp, d.bs, d.bt, d.bM, d.partials, d.p, d.pi2, d.si2, d.ppe_B,
+                    d.rowsum, d.ppe_val32, d.ppe_col, d.ij_count, d.s, (long long)c.npfb, c.npfb, c.itermax, c.tol,
+                    c.warm_start},
+             x.d_mg, (int)x.mg.size(), tail, d.cellpart, d.cell_start, d.cell_cnt, d.ip, (float*)x.mg_z,
+             (float*)x.mg_fr, (float*)x.mg_dinv0};
+  if (c.open_domain == 0) cudaLaunchKernelEx(&cfg, k_bicgstab_mixed_mg<true>, m);
+  else cudaLaunchKernelEx(&cfg, k_bicgstab_mixed_mg<false>, m);
+  x.launches++;
+}
+
 void launch_ppe_mg(Ctx& x) {
   const Consts& c = x.c;
   const Dev& d = x.d;
   const int nl = (int)x.mg.size();
-  VEBI_LAUNCH(x, k_mg_level1, grid_for(x.mg[0].n), TPB, c, d, x.mg[0]);
-  for (int l = 0; l + 1 < nl; ++l) VEBI_LAUNCH(x, k_mg_coarsen, grid_for(x.mg[l + 1].n), TPB, x.mg[l], x.mg[l + 1], d.s);
-  int tail = nl - 1;
-  for (int l = 0; l < nl; ++l)
-    if (x.mg[l].n <= MG_BLOCK_ROWS) { tail = l; break; }
+  const int tail = mg_setup(x);
   int nblk = x.mg_blocks;
   const long long rows_per_block = (long long)TPB * (x.solver_rows_per_thread > 0 ? x.solver_rows_per_thread : 1);
   long long need = (c.npfb + rows_per_block - 1) / rows_per_block;

@@ -340,53 +340,6 @@ void launch_ppe(Ctx& x) {
 // of 12 B, and performs no FP64 operation in the SpMV.
 namespace vebi {
 
-struct MxArgs {
-  double *x, *r, *rb, *v, *p, *s, *t, *rinvM, *part, *P;
-  float2 *pi, *si;                     // p_inv, s_inv as (hi, lo)
-  const double *B, *rs;                // right-hand side, FP64 row sums
-  const float* val32;
-  const int *col, *cnt;
-  Scal* sc;
-  long long stride;
-  int n, itermax;
-  double tol;
-  int warm;
-};
-
-__device__ __forceinline__ float2 split2(double v) {
-  float h = (float)v;
-  return make_float2(h, (float)(v - (double)h));
-}
-__device__ __forceinline__ double join2(float2 q) { return (double)q.x + (double)q.y; }
-
-__device__ __forceinline__ double spmv_diff32(const MxArgs& a, const float2* xv, int i) {
-  const int cnt = __ldg(a.cnt + i);
-  const float* vp = a.val32 + i;
-  const int* cp = a.col + i;
-  const long long st = a.stride;
-  const float2 xi = __ldca(xv + i);
-  float b0 = 0.0f, b1 = 0.0f, b2 = 0.0f, b3 = 0.0f;
-  int k = 0;
-  for (; k + 3 < cnt; k += 4) {
-    const int c0 = __ldg(cp), c1 = __ldg(cp + st), c2 = __ldg(cp + 2 * st), c3 = __ldg(cp + 3 * st);
-    const float v0 = __ldg(vp), v1 = __ldg(vp + st), v2 = __ldg(vp + 2 * st), v3 = __ldg(vp + 3 * st);
-    const float2 x0 = __ldca(xv + c0), x1 = __ldca(xv + c1), x2 = __ldca(xv + c2), x3 = __ldca(xv + c3);
-    b0 = fmaf(v0, (x0.x - xi.x) + (x0.y - xi.y), b0);
-    b1 = fmaf(v1, (x1.x - xi.x) + (x1.y - xi.y), b1);
-    b2 = fmaf(v2, (x2.x - xi.x) + (x2.y - xi.y), b2);
-    b3 = fmaf(v3, (x3.x - xi.x) + (x3.y - xi.y), b3);
-    cp += 4 * st;
-    vp += 4 * st;
-  }
-  for (; k < cnt; ++k) {
-    const float2 x0 = __ldca(xv + __ldg(cp));
-    b0 = fmaf(__ldg(vp), (x0.x - xi.x) + (x0.y - xi.y), b0);
-    cp += st;
-    vp += st;
-  }
-  return fma(__ldg(a.rs + i), join2(xi), (double)((b0 + b1) + (b2 + b3)));
-}
-
 template <bool NONULL>
 __global__ void __launch_bounds__(TPB, 5) k_bicgstab_mixed(MxArgs a) {
   __shared__ double sh[64];
@@ -551,9 +504,15 @@ int ppe_mixed_blocks(int nsm) {
   return per * nsm;
 }
 
+void launch_ppe_mg_mixed(Ctx& x);
+
 void launch_ppe_mixed_solve(Ctx& x) {
   const Consts& c = x.c;
   VEBI_LAUNCH(x, k_matrix_mixed, grid_for(c.npfb), TPB, c, x.d);
+  if (c.precond) {
+    launch_ppe_mg_mixed(x);
+    return;
+  }
   int nblk = x.coop_blocks_mixed;
   const long long rows_per_block = (long long)TPB * (x.solver_rows_per_thread > 0 ? x.solver_rows_per_thread : 1);
   long long need = (c.npfb + rows_per_block - 1) / rows_per_block;

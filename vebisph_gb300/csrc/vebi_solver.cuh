@@ -115,4 +115,52 @@ __device__ __forceinline__ double spmv_row(const BiArgs& a, const double* xv, in
   return (b0 + b1) + (b2 + b3);
 }
 
+// ---- mixed precision: FP64 recurrences, FP32 difference-form SpMV (see vebi_ppe.cu)
+struct MxArgs {
+  double *x, *r, *rb, *v, *p, *s, *t, *rinvM, *part, *P;
+  float2 *pi, *si;                     // p_inv, s_inv as (hi, lo)
+  const double *B, *rs;                // right-hand side, FP64 row sums
+  const float* val32;
+  const int *col, *cnt;
+  Scal* sc;
+  long long stride;
+  int n, itermax;
+  double tol;
+  int warm;
+};
+
+__device__ __forceinline__ float2 split2(double v) {
+  float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
+__device__ __forceinline__ double join2(float2 q) { return (double)q.x + (double)q.y; }
+
+__device__ __forceinline__ double spmv_diff32(const MxArgs& a, const float2* xv, int i) {
+  const int cnt = __ldg(a.cnt + i);
+  const float* vp = a.val32 + i;
+  const int* cp = a.col + i;
+  const long long st = a.stride;
+  const float2 xi = __ldca(xv + i);
+  float b0 = 0.0f, b1 = 0.0f, b2 = 0.0f, b3 = 0.0f;
+  int k = 0;
+  for (; k + 3 < cnt; k += 4) {
+    const int c0 = __ldg(cp), c1 = __ldg(cp + st), c2 = __ldg(cp + 2 * st), c3 = __ldg(cp + 3 * st);
+    const float v0 = __ldg(vp), v1 = __ldg(vp + st), v2 = __ldg(vp + 2 * st), v3 = __ldg(vp + 3 * st);
+    const float2 x0 = __ldca(xv + c0), x1 = __ldca(xv + c1), x2 = __ldca(xv + c2), x3 = __ldca(xv + c3);
+    b0 = fmaf(v0, (x0.x - xi.x) + (x0.y - xi.y), b0);
+    b1 = fmaf(v1, (x1.x - xi.x) + (x1.y - xi.y), b1);
+    b2 = fmaf(v2, (x2.x - xi.x) + (x2.y - xi.y), b2);
+    b3 = fmaf(v3, (x3.x - xi.x) + (x3.y - xi.y), b3);
+    cp += 4 * st;
+    vp += 4 * st;
+  }
+  for (; k < cnt; ++k) {
+    const float2 x0 = __ldca(xv + __ldg(cp));
+    b0 = fmaf(__ldg(vp), (x0.x - xi.x) + (x0.y - xi.y), b0);
+    cp += st;
+    vp += st;
+  }
+  return fma(__ldg(a.rs + i), join2(xi), (double)((b0 + b1) + (b2 + b3)));
+}
+
 }  // namespace vebi
