@@ -234,6 +234,9 @@ static int allocate_all(Ctx& x) {
   A_(d.gpx, n); A_(d.gpy, n);
   if (x.precision == VEBI_PREC_MIXED) {
     A_(d.ppe_val32, E); A_(d.rowsum, n); A_(d.pi2, n); A_(d.si2, n);
+    A_(d.hl_u[0], cap); A_(d.hl_u[1], cap); A_(d.hl_th, cap); A_(d.hl_us[0], cap); A_(d.hl_us[1], cap);
+    A_(d.hl_p, cap);
+    for (int q = 0; q < 4; ++q) A_(d.hl_tau[q], cap);
     A_(d.wGx32, E); A_(d.wGy32, E); A_(d.wL32, E);
     for (int q = 0; q < 4; ++q) A_(d.kgcm32[q], n);
   }

@@ -81,7 +81,7 @@ constexpr int MG_SLOTS = 24;
 constexpr int MG_ROW_SLOTS = 16;
 constexpr int MG_COARSEST = 32;
 constexpr int MG_MAX_LEVELS = 12;
-constexpr int MG_BLOCK_ROWS = 8192;
+constexpr int MG_BLOCK_ROWS = 2048;
 constexpr int MG_SWEEPS = 16;
 constexpr double MG_OMEGA = 0.9;
 constexpr double MG_GAMMA = 1.8;
@@ -135,6 +135,10 @@ struct Dev {
   float* ppe_val32;                          // FP32 off-diagonal values
   double* rowsum;                            // FP64 row sums of the PPE matrix
   float2 *pi2, *si2;                         // p_inv, s_inv as FP32 (hi, lo) pairs
+  // mixed precision: particle fields (fluid, walls and mirrors) as FP32 (hi, lo) pairs, so a
+  // pair difference f_j - f_i = (hi_j - hi_i) + (lo_j - lo_i) is formed in FP32 arithmetic
+  // with the accuracy of the FP64 difference rounded to FP32
+  float2 *hl_u[2], *hl_th, *hl_tau[4], *hl_us[2], *hl_p;
   float4* pk;                                // FP32 offset to the cell origin + cell coords
   float *wGx32, *wGy32, *wL32;               // FP32 pair weights (ELL)
   float* kgcm32[4];

@@ -10,6 +10,8 @@
 // The updates of u, theta and the positions stay FP64, and so do the log-conformation
 // eigen-step (k_logconf) and the PPE refinement.  The PPE matrix is assembled in FP64 from the
 // FP32 Morris weights, so the FP32 solver's matrix and the FP64 residual's matrix agree.
+#include <initializer_list>
+
 #include "vebi_ctx.cuh"
 
 namespace vebi {
@@ -137,16 +139,36 @@ __global__ void k_shift32(Consts c, Dev d) {
 }
 
 // grad_operator for u, v, theta in FP32 (gradient_calculation.F90:50-94)
+// FP64 fields of all np particles (fluid, walls, mirrors) as FP32 (hi, lo) pairs
+struct SplitArgs {
+  const double* src[4];
+  float2* dst[4];
+  int nf;
+};
+
+__global__ void k_split_fields(Dev d, SplitArgs a) {
+  const int np = d.s->np;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x)
+    for (int f = 0; f < a.nf; ++f) {
+      const double v = a.src[f][i];
+      const float h = (float)v;
+      a.dst[f][i] = make_float2(h, (float)(v - (double)h));
+    }
+}
+
+// f_j - f_i of two split values, in FP32
+__device__ __forceinline__ float dhl(float2 fj, float2 fi) { return (fj.x - fi.x) + (fj.y - fi.y); }
+
 __global__ void k_gradients32(Consts c, Dev d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.npfb) return;
-  const double ui = d.ux[i], vi = d.uy[i], ti = d.th[i];
+  const float2 ui = d.hl_u[0][i], vi = d.hl_u[1][i], ti = d.hl_th[i];
   float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f, a4 = 0.f, a5 = 0.f;
   const int cnt = d.ij_count[i];
   for (int k = 0; k < cnt; ++k) {
     int j = d.ij_link[ELL(k, i)];
     float w1 = d.wGx32[ELL(k, i)], w2 = d.wGy32[ELL(k, i)];
-    float du = (float)(d.ux[j] - ui), dvv = (float)(d.uy[j] - vi), dth = (float)(d.th[j] - ti);
+    float du = dhl(d.hl_u[0][j], ui), dvv = dhl(d.hl_u[1][j], vi), dth = dhl(d.hl_th[j], ti);
     a0 = fmaf(du, w1, a0);
     a1 = fmaf(du, w2, a1);
     a2 = fmaf(dvv, w1, a2);
@@ -168,21 +190,22 @@ __global__ void k_predictor32(Consts c, Dev d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.npfb) return;
   const double ui = d.ux[i], vi = d.uy[i], ti = d.th[i];
+  const float2 hu = d.hl_u[0][i], hv = d.hl_u[1][i], ht = d.hl_th[i];
   const float K11 = d.kgcm32[0][i], K21 = d.kgcm32[1][i], K12 = d.kgcm32[2][i], K22 = d.kgcm32[3][i];
   const bool ve = c.const_mod != 1;
-  double Ti11 = 0, Ti21 = 0, Ti12 = 0, Ti22 = 0;
-  if (ve) { Ti11 = d.tau[0][i]; Ti21 = d.tau[1][i]; Ti12 = d.tau[2][i]; Ti22 = d.tau[3][i]; }
+  float2 Ti11 = make_float2(0.f, 0.f), Ti21 = Ti11, Ti12 = Ti11, Ti22 = Ti11;
+  if (ve) { Ti11 = d.hl_tau[0][i]; Ti21 = d.hl_tau[1][i]; Ti12 = d.hl_tau[2][i]; Ti22 = d.hl_tau[3][i]; }
   const float cs = (float)c.coeff_solvent, cp = (float)c.coeff_polymeric, ct = (float)c.coeff_theta;
   float s1 = 0.f, s2 = 0.f, st = 0.f;
   const int cnt = d.ij_count[i];
   for (int k = 0; k < cnt; ++k) {
     int j = d.ij_link[ELL(k, i)];
-    float u1 = (float)(ui - d.ux[j]), u2 = (float)(vi - d.uy[j]);
+    float u1 = dhl(hu, d.hl_u[0][j]), u2 = dhl(hv, d.hl_u[1][j]);
     float wl = d.wL32[ELL(k, i)];
     if (ve) {
       float w1 = d.wGx32[ELL(k, i)], w2 = d.wGy32[ELL(k, i)];
-      float T11 = (float)(d.tau[0][j] - Ti11), T21 = (float)(d.tau[1][j] - Ti21);
-      float T12 = (float)(d.tau[2][j] - Ti12), T22 = (float)(d.tau[3][j] - Ti22);
+      float T11 = dhl(d.hl_tau[0][j], Ti11), T21 = dhl(d.hl_tau[1][j], Ti21);
+      float T12 = dhl(d.hl_tau[2][j], Ti12), T22 = dhl(d.hl_tau[3][j], Ti22);
       float kw1 = fmaf(K11, w1, K12 * w2), kw2 = fmaf(K21, w1, K22 * w2);
       float tw1 = fmaf(T11, kw1, T12 * kw2), tw2 = fmaf(T21, kw1, T22 * kw2);
       s1 = fmaf(cp, tw1, fmaf(cs * u1, wl, s1));
@@ -191,7 +214,7 @@ __global__ void k_predictor32(Consts c, Dev d) {
       s1 = fmaf(cs * u1, wl, s1);
       s2 = fmaf(cs * u2, wl, s2);
     }
-    float thij = (float)(ti - d.th[j]);
+    float thij = dhl(ht, d.hl_th[j]);
     st = fmaf(ct * thij, wl, st);
   }
   const double dt = d.s->dt;
@@ -213,13 +236,13 @@ __global__ void k_ppe_rhs32(Consts c, Dev d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   double b = 0.0;
   if (i < c.npfb) {
-    const double ui = d.ux2[i], vi = d.uy2[i];
+    const float2 ui = d.hl_us[0][i], vi = d.hl_us[1][i];
     const float K11 = d.kgcm32[0][i], K21 = d.kgcm32[1][i], K12 = d.kgcm32[2][i], K22 = d.kgcm32[3][i];
     float fb = 0.f;
     const int cnt = d.ij_count[i];
     for (int k = 0; k < cnt; ++k) {
       int j = d.ij_link[ELL(k, i)];
-      float u1 = (float)(ui - d.ux2[j]), u2 = (float)(vi - d.uy2[j]);
+      float u1 = dhl(ui, d.hl_us[0][j]), u2 = dhl(vi, d.hl_us[1][j]);
       float w1 = d.wGx32[ELL(k, i)], w2 = d.wGy32[ELL(k, i)];
       float kw1 = fmaf(K11, w1, K12 * w2), kw2 = fmaf(K21, w1, K22 * w2);
       fb = fb - fmaf(u1, kw1, u2 * kw2);
@@ -237,11 +260,12 @@ __global__ void k_pgrad_final32(Consts c, Dev d) {
   double mu = -1.0, mv = -1.0, mp = -1.0;
   if (i < c.npfb) {
     const double pi_ = d.p[i];
+    const float2 hp = d.hl_p[i];
     float a = 0.f, b = 0.f;
     const int cnt = d.ij_count[i];
     for (int k = 0; k < cnt; ++k) {
       int j = d.ij_link[ELL(k, i)];
-      float temp = (float)(d.p[j] - pi_);
+      float temp = dhl(d.hl_p[j], hp);
       a = fmaf(temp, d.wGx32[ELL(k, i)], a);
       b = fmaf(temp, d.wGy32[ELL(k, i)], b);
     }
@@ -279,9 +303,32 @@ __global__ void k_pgrad_final32(Consts c, Dev d) {
 // the cell-relative offsets d.pk are written by the neighbour search (vebi_cells.cu)
 void launch_prep_weights32(Ctx& x) { VEBI_LAUNCH(x, k_weights32, grid_for(x.c.npfb), TPB, x.c, x.d); }
 void launch_shift32(Ctx& x) { VEBI_LAUNCH(x, k_shift32, grid_for(x.c.npfb), TPB, x.c, x.d); }
-void launch_gradients32(Ctx& x) { VEBI_LAUNCH(x, k_gradients32, grid_for(x.c.npfb), TPB, x.c, x.d); }
-void launch_predictor32(Ctx& x) { VEBI_LAUNCH(x, k_predictor32, grid_for(x.c.npfb), TPB, x.c, x.d); }
-void launch_ppe_rhs32(Ctx& x) { VEBI_LAUNCH(x, k_ppe_rhs32, grid_for(x.c.npfb), TPB, x.c, x.d); }
-void launch_pgrad_final32(Ctx& x) { VEBI_LAUNCH(x, k_pgrad_final32, grid_for(x.c.npfb), TPB, x.c, x.d); }
+static void split(Ctx& x, std::initializer_list<const double*> src, std::initializer_list<float2*> dst) {
+  SplitArgs a{};
+  int f = 0;
+  for (const double* p : src) a.src[f++] = p;
+  a.nf = f;
+  f = 0;
+  for (float2* p : dst) a.dst[f++] = p;
+  VEBI_LAUNCH(x, k_split_fields, x.gs_blocks, TPB, x.d, a);
+}
+
+void launch_gradients32(Ctx& x) {
+  split(x, {x.d.ux, x.d.uy, x.d.th}, {x.d.hl_u[0], x.d.hl_u[1], x.d.hl_th});  // also read by the predictor
+  VEBI_LAUNCH(x, k_gradients32, grid_for(x.c.npfb), TPB, x.c, x.d);
+}
+void launch_predictor32(Ctx& x) {
+  if (x.c.const_mod != 1)  // tau after the log-conformation update and the mirror stresses
+    split(x, {x.d.tau[0], x.d.tau[1], x.d.tau[2], x.d.tau[3]}, {x.d.hl_tau[0], x.d.hl_tau[1], x.d.hl_tau[2], x.d.hl_tau[3]});
+  VEBI_LAUNCH(x, k_predictor32, grid_for(x.c.npfb), TPB, x.c, x.d);
+}
+void launch_ppe_rhs32(Ctx& x) {
+  split(x, {x.d.ux2, x.d.uy2}, {x.d.hl_us[0], x.d.hl_us[1]});  // u* with the mirrors' u*
+  VEBI_LAUNCH(x, k_ppe_rhs32, grid_for(x.c.npfb), TPB, x.c, x.d);
+}
+void launch_pgrad_final32(Ctx& x) {
+  split(x, {x.d.p}, {x.d.hl_p});  // P with the mirrors' P
+  VEBI_LAUNCH(x, k_pgrad_final32, grid_for(x.c.npfb), TPB, x.c, x.d);
+}
 
 }  // namespace vebi
