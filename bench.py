@@ -18,6 +18,7 @@ not shard); `value` sums the ranks' particle-steps over the slowest rank's time.
 from __future__ import annotations
 
 import argparse
+import copy
 import json
 import os
 import pathlib
@@ -323,6 +324,9 @@ def run_batch(args, dist: Dist):
     from vebisph_gb300.solver import BatchSolver, StepSolver, VebiError
 
     cl = cases.batch_sweep(args.batch, seed=args.seed)
+    mg = args.batch_precond == "multigrid"
+    for c in cl:
+        c.ppe_precond = abi.PRECOND_MULTIGRID if mg else abi.PRECOND_NONE
     n_fluid = sum(c.n_fluid for c in cl)
     t0 = time.perf_counter()
     bprec = abi.PREC_MIXED if args.batch_precision == "mixed" else abi.PREC_FP64
@@ -346,7 +350,7 @@ def run_batch(args, dist: Dist):
     n_live = sum(c.n_fluid for i, c in enumerate(cl) if i not in failed)
     value = dist.sum(float(n_live * args.steps)) / (t_max * 1e-3)
     # the same instances one by one, plain FP64, timed over the same K steps (device events)
-    serial_ms, serial_units, du, dp, per = 0.0, 0, [], [], []
+    serial_ms, serial_units, du, dp, per, spread = 0.0, 0, [], [], [], []
     for i, (c, fm) in enumerate(zip(cl, fields)):
         s1 = StepSolver(c, precision=abi.PREC_FP64)
         rec = {"i": i, "case": c.name, "n_fluid": c.n_fluid, "El": c.El, "beta": c.beta,
@@ -369,12 +373,42 @@ def run_batch(args, dist: Dist):
                     rec["du"] = float("inf")
                 du.append(rec["du"])
                 dp.append(rec["dp"])
+                # the flow's own sensitivity: FP64 again from a velocity perturbed at FP32 rounding
+                # level (relative 6e-8, seeded), same steps
+                cp_ = copy.deepcopy(c)
+                rng = np.random.default_rng(1000 + i)
+                cp_.u = cp_.u * (1.0 + 6e-8 * rng.standard_normal(cp_.u.shape))
+                s2 = StepSolver(cp_, precision=abi.PREC_FP64)
+                try:
+                    for _ in range(done):
+                        s2.step()
+                    vx, vy = (s2.get(k)[: c.npfb] for k in ("ux", "uy"))
+                    rec["fp64_spread"] = float(max(np.abs(vx - ux).max(), np.abs(vy - uy).max()) / us)
+                except VebiError:
+                    rec["fp64_spread"] = float("inf")
+                s2.close()
+                spread.append(rec["fp64_spread"])
         except VebiError as e:
             rec["fp64_error"] = e.status
         s1.close()
         per.append(rec)
     serial_value = serial_units / (serial_ms * 1e-3)
-    du, dp = np.array(du), np.array(dp)
+    plain = None
+    if mg:  # the reference's solver one by one: K steps from the initial state (speed only)
+        pms, punits = 0.0, 0
+        for c in cases.batch_sweep(args.batch, seed=args.seed):
+            s1 = StepSolver(c, precision=abi.PREC_FP64)
+            try:
+                m1, _ = s1.run_steps(args.steps)
+                pms += m1
+                punits += c.n_fluid * args.steps
+            except VebiError:
+                pass
+            s1.close()
+        plain = {"value": punits / (pms * 1e-3), "unit": UNIT, "ms_per_step": pms / args.steps,
+                 "path": "one StepSolver per instance, plain FP64, unpreconditioned PPE (the reference's solver), "
+                         f"{args.steps} steps from the initial state"}
+    du, dp, spread = np.array(du), np.array(dp), np.array(spread)
     counts = np.array([c.n_fluid for c in cl])
     try:
         (ROOT / "gpurun_out").mkdir(exist_ok=True)
@@ -388,7 +422,7 @@ def run_batch(args, dist: Dist):
         "data": "synthetic: seeded jittered lattices, walls/circle by the reference's make_boundary_particles rules",
         "config": {"workload": f"batch{args.batch}: {args.batch} independent instances (even: Poiseuille channel, "
                                f"odd: confined cylinder), fluid counts log-uniform 4k-256k, Wi~U[0.1,4], "
-                               f"beta~U[0.1,0.9], seed {args.seed}, {args.batch_precision}",
+                               f"beta~U[0.1,0.9], seed {args.seed}, {args.batch_precision}, PPE preconditioner {args.batch_precond}",
                    "instances": args.batch, "n_fluid_total": n_fluid,
                    "n_fluid_min": int(counts.min()), "n_fluid_max": int(counts.max()),
                    "parallelism": f"batch (one CUDA graph per step, {args.batch} branches) x{dist.world} replicas",
@@ -401,12 +435,19 @@ def run_batch(args, dist: Dist):
                              "statuses": sorted(set(failed.values()))},
         "serial_fp64": {"value": serial_value, "unit": UNIT, "ms_per_step": serial_ms / args.steps,
                         "speedup_of_batch": value / serial_value, "counted": "instances that did not fail",
-                        "path": "one StepSolver per instance, FP64, graph-replayed steps, summed device time"},
+                        "path": "one StepSolver per instance, FP64, same PPE preconditioner as the batch, "
+                                "graph-replayed steps, summed device time"},
+        "serial_plain_fp64": plain,
+        "speedup_vs_serial_plain_fp64": (value / plain["value"]) if plain else None,
         "batch_vs_serial_fp64": ({
             "compared": int(du.size), "note": "instances where neither run failed; u = max|du|/max|u_fp64|",
             "u_rel_median": float(np.median(du)), "u_rel_p90": float(np.percentile(du, 90)),
             "u_within_1e-4": int((du <= 1e-4).sum()), "u_within_1e-3": int((du <= 1e-3).sum()),
-            "u_within_1e-2": int((du <= 1e-2).sum()), "p_rel_median": float(np.median(dp))}
+            "u_within_1e-2": int((du <= 1e-2).sum()), "p_rel_median": float(np.median(dp)),
+            "fp64_spread_median": float(np.median(spread)),
+            "u_within_max_1e-4_2x_fp64_spread": int((du <= np.maximum(1e-4, 2.0 * spread)).sum()),
+            "spread_note": "fp64_spread: FP64 rerun from velocities perturbed by 6e-8 relative (FP32 rounding) "
+                           "after the same steps; the flow's own amplification of rounding-level differences"}
             if du.size else None),
         "roofline": None,
         "clocks": clk.summary(),
@@ -529,6 +570,7 @@ def main():
     ap.add_argument("--batch", type=int, default=0,
                     help="run the batched parameter sweep of this many instances instead")
     ap.add_argument("--batch-precision", choices=["fp64", "mixed"], default="mixed")
+    ap.add_argument("--batch-precond", choices=["none", "multigrid"], default="multigrid")
     ap.add_argument("--tune", default="1,2,4", help="solver rows-per-thread candidates of the batch autotuner")
     ap.add_argument("--warm-start", action="store_true",
                     help="opt-in: PPE starts from the previous step's pressure (changes results)")

@@ -14,13 +14,20 @@ def _cases():
             cases.poiseuille(20, seed=4, const_mod=1), cases.cylinder(1.2e4, Wi=1.5, seed=5, beta=0.8)]
 
 
+def _with_precond(cl, pc):
+    for c in cl:
+        c.ppe_precond = pc
+    return cl
+
+
 @pytest.mark.parametrize("prec", [abi.PREC_FP64, abi.PREC_MIXED])
-def test_batch_equals_individual_runs(built, prec):
+@pytest.mark.parametrize("pc", [abi.PRECOND_NONE, abi.PRECOND_MULTIGRID])
+def test_batch_equals_individual_runs(built, prec, pc):
     from vebisph_gb300.solver import BatchSolver, StepSolver
-    b = BatchSolver(_cases(), precision=prec)
+    b = BatchSolver(_with_precond(_cases(), pc), precision=prec)
     ms, stats = b.step(3)
     assert ms > 0 and len(stats) == 6
-    for i, c in enumerate(_cases()):
+    for i, c in enumerate(_with_precond(_cases(), pc)):
         s = StepSolver(c, precision=prec)
         for _ in range(3):
             si = s.step()

@@ -182,6 +182,8 @@ __global__ void k_cell_offsets(Consts c, Dev d) {
 // at most ~6 eps S, so |r^2_32 - r^2| < ~32 eps S^2 = 32 eps sup_size_2; the band below is
 // 64 eps sup_size_2 (eps = 2^-24), so every pair inside it is re-tested exactly and the list
 // equals the FP64 list.
+constexpr int NB_UNROLL = 4;
+
 __global__ void k_neighbours(Consts c, Dev d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.npfb) return;
@@ -215,24 +217,36 @@ __global__ void k_neighbours(Consts c, Dev d) {
       int jc = jcs[q];
       if (jc < 1 || jc > c.nct) continue;  // cells past the grid are empty in the reference
       int cc = jc - 1;
-      int s0 = d.cell_start[cc], s1 = s0 + d.cell_cnt[cc];
-      for (int jj = s0; jj < s1; ++jj) {
-        int j = d.ip[jj];
-        const float4 pj = d.pk[j];
-        const float f1 = (pi.x - pj.x) + (pi.z - pj.z) * S, f2 = (pi.y - pj.y) + (pi.w - pj.w) * S;
-        const float q = fmaf(f1, f1, f2 * f2);
-        bool take;
-        if (q > S2 + band) take = false;
-        else if (q < S2 - band && q > band) take = true;
-        else {  // near a threshold: the reference's FP64 test
-          double r1 = xi - d.rx[j], r2 = yi - d.ry[j];
-          double rr2 = r1 * r1 + r2 * r2;
-          take = rr2 > 0.0 && rr2 <= c.sup_size_2;
-        }
-        if (take) {
-          if (cnt < c.nplink) d.ij_link[(size_t)cnt * c.npfb + i] = j;
-          else over = true;
-          ++cnt;
+      int s0 = __ldg(d.cell_start + cc), s1 = s0 + __ldg(d.cell_cnt + cc);
+      // candidates NB_UNROLL at a time: their index and position loads are issued together
+      for (int jj = s0; jj < s1; jj += NB_UNROLL) {
+        int jv[NB_UNROLL];
+        float4 pv[NB_UNROLL];
+#pragma unroll
+        for (int u = 0; u < NB_UNROLL; ++u) jv[u] = jj + u < s1 ? __ldg(d.ip + jj + u) : -1;
+#pragma unroll
+        for (int u = 0; u < NB_UNROLL; ++u)
+          pv[u] = jv[u] >= 0 ? __ldg(d.pk + jv[u]) : make_float4(0.f, 0.f, 1.0e6f, 1.0e6f);
+#pragma unroll
+        for (int u = 0; u < NB_UNROLL; ++u) {
+          const int j = jv[u];
+          if (j < 0) break;
+          const float4 pj = pv[u];
+          const float f1 = (pi.x - pj.x) + (pi.z - pj.z) * S, f2 = (pi.y - pj.y) + (pi.w - pj.w) * S;
+          const float q = fmaf(f1, f1, f2 * f2);
+          bool take;
+          if (q > S2 + band) take = false;
+          else if (q < S2 - band && q > band) take = true;
+          else {  // near a threshold: the reference's FP64 test
+            double r1 = xi - d.rx[j], r2 = yi - d.ry[j];
+            double rr2 = r1 * r1 + r2 * r2;
+            take = rr2 > 0.0 && rr2 <= c.sup_size_2;
+          }
+          if (take) {
+            if (cnt < c.nplink) d.ij_link[(size_t)cnt * c.npfb + i] = j;
+            else over = true;
+            ++cnt;
+          }
         }
       }
     }
