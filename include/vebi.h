@@ -216,6 +216,32 @@ int vebi_ppe_solve_noalloc(const int32_t* ij_count, const int32_t* ppe_col, cons
                            int64_t ell_stride, int32_t closed_domain, double tol, int32_t itermax,
                            void* stream, int32_t* iters_out, double* residual_out);
 
+/* ---- Output files (output.F90:18-85) -------------------------------------------------
+ * vebi_dump_async snapshots the particle fields after the last step and copies them to pinned
+ * host memory on a stream of its own, overlapping the following steps.  vebi_dump_write waits
+ * for those copies and writes, in the reference's gfortran list-directed layout:
+ *  - part_path: a PART dump (output.F90:40-51; inbin particles skipped, no mirrors as
+ *    output_mirrors is .false., div_free.F90:36);
+ *  - restart_path: the TEMP_REC.dat restart record (output.F90:59-77).
+ * Either path may be NULL.  With VEBI_DUMP_BACKGROUND the files are written on a host thread
+ * and the call returns at once; vebi_dump_wait joins it (the next vebi_dump_async does too).
+ * VEBI_DUMP_RESTART_READABLE (opt-in) writes the restart particle lines without theta, the
+ * layout the reference's restart reader expects (input.F90:123-126): the reference writes
+ * theta (output.F90:70) but does not read it back.
+ * vebi_format_list formats one list-directed record ('r' real(8), 'i' integer(4) items) with
+ * its newline, as the reference's TIME / LS / TIME_OUT lines (output.F90:56,84-85); returns the
+ * length, or -1 when cap is too small. */
+#define VEBI_DUMP_BACKGROUND 1
+#define VEBI_DUMP_RESTART_READABLE 2
+typedef struct vebi_dump_info {
+  double time, dt, xb_min, xb_max, yb_min, yb_max, dx, av_conc, dv;
+  int32_t itime, n_dump, np_inflow, flags;
+} vebi_dump_info;
+int vebi_dump_async(vebi_ctx* ctx);
+int vebi_dump_write(vebi_ctx* ctx, const vebi_dump_info* info, const char* part_path, const char* restart_path);
+int vebi_dump_wait(vebi_ctx* ctx);
+int64_t vebi_format_list(const char* kinds, const double* reals, const int32_t* ints, char* out, int64_t cap);
+
 /* ---- Batches of independent simulations ----------------------------------------------
  * No counterpart in the reference, which runs one simulation per process.  A batch owns n
  * contexts (one per simulation, each with its own device arrays); uneven particle counts and

@@ -5,6 +5,9 @@ rb_deck_digest.json: SHA-256 digests and scalars of the case deck shipped with t
   vebisph_gb300.cases.read_deck.  tests/test_cases.py checks that the restated generator
   vebisph_gb300.cases.rayleigh_benard_deck() reproduces these digests bit for bit.
 oracle_rb_step1.json: a regression summary of one oracle step on that deck.
+list_directed.json: the SHA-256 of the shipped IPART text (gfortran list-directed real(8)
+  output, datclass.F90:649-651) and sample lines of it and of IBOUND (integer items,
+  datclass.F90:686-700): the golden vectors of the library's list-directed formatter.
 
 Usage: python tests/golden/make_fixtures.py [/path/to/reference]
 """
@@ -47,12 +50,23 @@ def oracle_summary(c: cases.Case) -> dict:
                 vrelation=digest(o.get("vrelation")), max_abs_p=s["max_abs_p"], max_abs_v=s["max_abs_v"])
 
 
+def list_directed_summary(gen: pathlib.Path) -> dict:
+    ipart = (gen / "IPART").read_bytes()
+    lines = ipart.decode().splitlines()
+    ibound = (gen / "IBOUND").read_text().splitlines()
+    ints = [ln[:12] for ln in ibound if ln[:12].strip().lstrip("-").isdigit()]
+    return dict(ipart_sha256=hashlib.sha256(ipart).hexdigest(), ipart_lines=len(lines),
+                ipart_sample={str(i): lines[i] for i in (0, 1, 2, 100, 201, 202, 5000, len(lines) - 1)},
+                ibound_integer_items=ints)
+
+
 def main():
     ref = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     deck = cases.read_deck(ref / "source" / "gen")
     (HERE / "rb_deck_digest.json").write_text(json.dumps(deck_summary(deck), indent=1) + "\n")
     (HERE / "oracle_rb_step1.json").write_text(json.dumps(oracle_summary(deck), indent=1) + "\n")
-    print("wrote", HERE / "rb_deck_digest.json", HERE / "oracle_rb_step1.json")
+    (HERE / "list_directed.json").write_text(json.dumps(list_directed_summary(ref / "source" / "gen"), indent=1) + "\n")
+    print("wrote", HERE / "rb_deck_digest.json", HERE / "oracle_rb_step1.json", HERE / "list_directed.json")
 
 
 if __name__ == "__main__":

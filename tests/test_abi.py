@@ -15,7 +15,7 @@ ROOT = pathlib.Path(__file__).resolve().parent.parent
 def header_functions():
     txt = (ROOT / "include" / "vebi.h").read_text()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(vebi_\w+)\s*\(", txt, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(vebi_\w+)\s*\(", txt, flags=re.M)))
 
 
 def test_header_functions_listed():
@@ -33,10 +33,13 @@ def test_struct_layout_matches_header(tmp_path):
     src = tmp_path / "probe.c"
     fields_p = [f for f, _ in abi.VebiParams._fields_]
     fields_s = [f for f, _ in abi.VebiStepStats._fields_]
+    fields_d = [f for f, _ in abi.VebiDumpInfo._fields_]
     body = ['#include <stdio.h>', '#include <stddef.h>', '#include "vebi.h"', 'int main(void){',
             'printf("%zu %zu\\n", sizeof(vebi_params), sizeof(vebi_step_stats));']
     body += [f'printf("%zu\\n", offsetof(vebi_params, {f}));' for f in fields_p]
     body += [f'printf("%zu\\n", offsetof(vebi_step_stats, {f}));' for f in fields_s]
+    body += ['printf("%zu\\n", sizeof(vebi_dump_info));']
+    body += [f'printf("%zu\\n", offsetof(vebi_dump_info, {f}));' for f in fields_d]
     body += ["return 0;}"]
     src.write_text("\n".join(body))
     exe = tmp_path / "probe"
@@ -47,7 +50,8 @@ def test_struct_layout_matches_header(tmp_path):
     assert ss == C.sizeof(abi.VebiStepStats)
     offs = list(map(int, out[2:]))
     want = [getattr(abi.VebiParams, f).offset for f in fields_p] + \
-           [getattr(abi.VebiStepStats, f).offset for f in fields_s]
+           [getattr(abi.VebiStepStats, f).offset for f in fields_s] + [C.sizeof(abi.VebiDumpInfo)] + \
+           [getattr(abi.VebiDumpInfo, f).offset for f in fields_d]
     assert offs == want
 
 

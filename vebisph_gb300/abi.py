@@ -64,6 +64,13 @@ class VebiParams(C.Structure):
     ]
 
 
+class VebiDumpInfo(C.Structure):
+    """vebi_dump_info of include/vebi.h: the host scalars of the dump files."""
+    _fields_ = [(k, C.c_double) for k in ("time", "dt", "xb_min", "xb_max", "yb_min", "yb_max", "dx", "av_conc",
+                                          "dv")] + \
+               [(k, C.c_int32) for k in ("itime", "n_dump", "np_inflow", "flags")]
+
+
 class VebiStepStats(C.Structure):
     _fields_ = [
         ("dt", C.c_double), ("LS_residual", C.c_double), ("umax", C.c_double),
@@ -102,7 +109,10 @@ EXPORTED_SYMBOLS = [
     "vebi_destroy", "vebi_pin_host", "vebi_unpin_host", "vebi_set_timing", "vebi_debug_size",
     "vebi_debug_get", "vebi_version", "vebi_last_error", "vebi_ppe_solve_noalloc",
     "vebi_batch_create", "vebi_batch_get", "vebi_batch_step", "vebi_batch_destroy", "vebi_set_solver_grid",
+    "vebi_dump_async", "vebi_dump_write", "vebi_dump_wait", "vebi_format_list",
 ]
+DUMP_BACKGROUND = 1
+DUMP_RESTART_READABLE = 2
 NOALLOC_MAX_ROWS = 65536
 
 _lib = None
@@ -148,6 +158,11 @@ def load_library():
     lib.vebi_batch_step.argtypes = [vp, C.c_int32, P(C.c_double), P(VebiStepStats)]
     lib.vebi_batch_destroy.argtypes = [vp]
     lib.vebi_set_solver_grid.argtypes = [vp, C.c_int32]
+    lib.vebi_dump_async.argtypes = [vp]
+    lib.vebi_dump_write.argtypes = [vp, P(VebiDumpInfo), C.c_char_p, C.c_char_p]
+    lib.vebi_dump_wait.argtypes = [vp]
+    lib.vebi_format_list.argtypes = [C.c_char_p, P(C.c_double), P(C.c_int32), C.c_char_p, C.c_int64]
+    lib.vebi_format_list.restype = C.c_int64
     for fn in ("vebi_batch_create", "vebi_batch_get", "vebi_batch_step", "vebi_batch_destroy", "vebi_set_solver_grid"):
         getattr(lib, fn).restype = C.c_int
     lib.vebi_version.restype = C.c_char_p

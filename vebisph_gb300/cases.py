@@ -490,3 +490,35 @@ def batch_sweep(n: int = 512, seed: int = 0, lo: float = 4.0e3, hi: float = 2.56
         else:
             out.append(cylinder(float(counts[k]), Wi=float(wis[k]), beta=float(betas[k]), seed=seed + k))
     return out
+
+
+def read_restart(path, const_mod: int = 2, theta: bool = True) -> dict:
+    """Read a TEMP_REC.dat restart record (output.F90:59-77; reader input.F90:119-136).
+
+    theta=True reads the particle lines as the reference writes them (theta included,
+    output.F90:70); theta=False reads the opt-in layout without theta that the reference's
+    reader expects (input.F90:123-126)."""
+    with open(path) as f:
+        head = [f.readline().split() for _ in range(3)]
+        rest = f.read().split()
+    itime, time, n_dump = int(head[0][0]), float(head[0][1]), int(head[0][2])
+    np_, npfb, nbS, np_inflow = (int(v) for v in head[1][:4])
+    box = [float(v) for v in head[2][:6]]
+    per = (8 if theta else 7) + (4 if const_mod != 1 else 0)
+    a = np.array(rest[: len(rest) - np_inflow], dtype=object).reshape(-1, per)
+    f64 = lambda col: np.array([float(v) for v in a[:, col]])  # noqa: E731
+    out = dict(itime=itime, time=time, n_dump=n_dump, np=np_, npfb=npfb, nbS=nbS, np_inflow=np_inflow,
+               xb_min=box[0], xb_max=box[1], yb_min=box[2], yb_max=box[3], dx=box[4], av_conc=box[5])
+    k = 0
+    out["r"] = np.stack([f64(0), f64(1)], 1)
+    out["u"] = np.stack([f64(2), f64(3)], 1)
+    k = 4
+    if theta:
+        out["theta"] = f64(4)
+        k = 5
+    out["p"] = f64(k)
+    out["dv"] = f64(k + 1)
+    out["n_surf"] = np.array([int(v) for v in a[:, k + 2]])
+    if const_mod != 1:  # tau_p(i,1,1), (1,2), (2,1), (2,2)
+        out["tau"] = np.stack([f64(k + 3 + q) for q in range(4)], 1)
+    return out

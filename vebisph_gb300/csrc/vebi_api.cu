@@ -14,6 +14,10 @@ int ppe_solver_blocks(int device, int nsm);
 int ppe_mixed_blocks(int nsm);
 int ppe_mg_blocks(int nsm);
 std::vector<int> mg_level_dims(int gx, int gy);
+void dump_free(Ctx& x);
+int dump_async(Ctx& x);
+int dump_write(Ctx& x, const vebi_dump_info* info, const char* part, const char* restart);
+int dump_wait(Ctx& x);
 
 static thread_local std::string g_err;
 
@@ -27,6 +31,8 @@ static int fail(int code, const std::string& msg) {
   g_err = msg;
   return code;
 }
+
+void vebi_set_error_text(const std::string& msg) { g_err = msg; }
 
 #define CUDA_TRY(expr)                                                              \
   do {                                                                              \
@@ -551,6 +557,7 @@ int vebi_destroy(vebi_ctx* h) {
   if (!h) return VEBI_OK;
   Ctx& x = h->x;
   if (x.st) cudaStreamSynchronize(x.st);
+  dump_free(x);
   for (auto& g : x.graph)
     if (g) cudaGraphExecDestroy(g);
   for (void* p : x.allocs) cudaFree(p);
@@ -587,6 +594,24 @@ int vebi_set_solver_grid(vebi_ctx* h, int32_t rows_per_thread) {
     x.graph_failed[m] = false;
   }
   return VEBI_OK;
+}
+
+int vebi_dump_async(vebi_ctx* h) {
+  if (!h) return fail(VEBI_ERR_ARG, "null context");
+  if (!h->x.have_state) return fail(VEBI_ERR_ARG, "no state uploaded");
+  int st = dump_async(h->x);
+  if (st == VEBI_ERR_CUDA) return fail(st, "dump staging failed");
+  return st;
+}
+
+int vebi_dump_write(vebi_ctx* h, const vebi_dump_info* info, const char* part_path, const char* restart_path) {
+  if (!h || !info) return fail(VEBI_ERR_ARG, "null argument");
+  return dump_write(h->x, info, part_path, restart_path);
+}
+
+int vebi_dump_wait(vebi_ctx* h) {
+  if (!h) return fail(VEBI_ERR_ARG, "null context");
+  return dump_wait(h->x);
 }
 
 int vebi_set_timing(vebi_ctx* h, int32_t on) {

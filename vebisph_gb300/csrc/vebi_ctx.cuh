@@ -9,6 +9,8 @@
 
 namespace vebi {
 
+struct DumpState;
+
 struct Ctx {
   vebi_params prm{};
   Consts c{};
@@ -43,6 +45,7 @@ struct Ctx {
   int *mg_ragg = nullptr, *mg_rcnt = nullptr;  // per-row (cell, value) pairs of the level-1 build
   double* mg_rval = nullptr;
   std::vector<void*> allocs;
+  DumpState* dump = nullptr;       // output staging (vebi_output.cu), made at the first dump
   vebi_step_stats last{};
 };
 

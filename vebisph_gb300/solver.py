@@ -117,6 +117,27 @@ class StepSolver:
     def set_solver_grid(self, rows_per_thread: int):
         self._check(self.lib.vebi_set_solver_grid(self.h, int(rows_per_thread)), "vebi_set_solver_grid")
 
+    # -- output files (output.F90) ------------------------------------------------------
+    def dump_async(self):
+        """Snapshot the fields after the last step; the host copies overlap later steps."""
+        self._check(self.lib.vebi_dump_async(self.h), "vebi_dump_async")
+
+    def dump_write(self, part_path=None, restart_path=None, *, time=0.0, dt=0.0, itime=0, n_dump=0,
+                   background=False, restart_readable=False, av_conc=0.0):
+        """Write the staged snapshot as a PART dump and/or a TEMP_REC.dat restart record."""
+        c = self.case
+        info = abi.VebiDumpInfo(time=time, dt=dt, xb_min=self.x_mint, xb_max=self.x_maxt, yb_min=self.y_mint,
+                                yb_max=self.y_maxt, dx=c.dx, av_conc=av_conc, dv=c.dv, itime=itime,
+                                n_dump=n_dump, np_inflow=0,
+                                flags=(abi.DUMP_BACKGROUND if background else 0) |
+                                      (abi.DUMP_RESTART_READABLE if restart_readable else 0))
+        enc = lambda p: None if p is None else str(p).encode()  # noqa: E731
+        self._check(self.lib.vebi_dump_write(self.h, C.byref(info), enc(part_path), enc(restart_path)),
+                    "vebi_dump_write")
+
+    def dump_wait(self):
+        self._check(self.lib.vebi_dump_wait(self.h), "vebi_dump_wait")
+
     def close(self):
         if getattr(self, "h", None):
             if self.owned:
