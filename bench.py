@@ -154,6 +154,43 @@ def ppe_bytes_per_iteration(n_rows: int, nnz_off: int, mixed: bool = False) -> f
     return 2.0 * (12.0 * nnz_off + 44.0 * n_rows) + 168.0 * n_rows
 
 
+def workload_text(args, case) -> str:
+    Re = (case.Ra / case.Pr) ** 0.5
+    common = (f"{case.n_fluid} fluid + {case.nbS} wall particles, dx={case.dx:.4g}, Oldroyd-B Re={Re:.3g} "
+              f"Wi={case.El * Re:.3g} beta={case.beta}, {args.precision}, PPE preconditioner {args.precond}")
+    if args.case == "cylinder_4m":
+        return f"{case.name}: confined cylinder, channel 30R x 4R, blockage 0.5, periodic x, " + common
+    if args.case.startswith("poiseuille"):
+        return f"{case.name}: planar Poiseuille channel 1x1, periodic x, walls y=0,1, body force, " + common
+    return f"{case.name}: " + common
+
+
+def stage_bandwidth(stage_ms_per_step: dict, n: int, kbar: float, mixed: bool, peak: float) -> dict:
+    """Per-stage achieved bandwidth on algorithmic bytes (each array the stage reads or writes
+    counted once per element, pair arrays at the mean neighbour count kbar, FP32-stored arrays at
+    4 B in the mixed step; a stage's several kernels share its time) over the stage's CUDA-event
+    time.  The FP64 pair stages are bound by the FP64 pipe (1.2 TFLOP/s on GB300), not HBM."""
+    w = 4.0 if mixed else 8.0
+    per_particle = {
+        "advect_bin": 90.0,
+        "neighbours": 16 + 4 + 4 * kbar + 4,
+        "weights": (4 + 3 * w) * kbar + 48,
+        "shifting": (4 + 2 * w) * kbar + 64,
+        "gradients": (4 + 2 * w) * kbar + 168,   # the three gradient calls fused: one pass over the pairs
+        "logconf": 120.0,
+        "predictor": (4 + 3 * w) * kbar + 160,
+        "ppe_assembly": (24 + 3 * w) * kbar + 84,  # right-hand side, then the matrix (FP64 value + column)
+        "pressure_grad": (4 + 2 * w) * kbar + 56,
+    }
+    out = {}
+    for k, b in per_particle.items():
+        ms = stage_ms_per_step.get(k)
+        if ms:
+            gbs = b * n / (ms * 1e-3) / 1e9
+            out[k] = {"bytes_per_particle": round(b, 1), "ms": ms, "GB_s": round(gbs, 1), "frac": round(gbs / peak, 4)}
+    return out
+
+
 def mg_bytes_per_iteration(n_rows: int, nnz_off: int, n_cells: int, mixed: bool = False) -> float:
     """Algorithmic bytes of one multigrid-preconditioned BiCGSTAB iteration (closed domain): the
     unpreconditioned iteration, plus 16 B per row for the mean corrections (row sums), plus two
@@ -197,6 +234,9 @@ def run_gb300(args, dist: Dist):
     import ctypes as C
 
     case = make_case(args)
+    if getattr(args, "perturb", 0.0):  # fluid positions moved by args.perturb * dx (seeded)
+        rng = np.random.default_rng(12345)
+        case.r[case.nbS:] = case.r[case.nbS:] + args.perturb * case.dx * rng.standard_normal(case.r[case.nbS:].shape)
     if args.itermax:
         case.itermax = args.itermax
     case.ppe_warm_start = 1 if args.warm_start else 0
@@ -295,15 +335,15 @@ def run_gb300(args, dist: Dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == abi.PREC_FP64 else "f32+f64",
         "data": "synthetic: seeded jittered lattice (U(-0.01dx,0.01dx)), walls/circle by the reference's "
                 "make_boundary_particles rules; no dataset",
-        "config": {"workload": f"{case.name}: confined cylinder, channel 30R x 4R, blockage 0.5, "
-                               f"{n_fluid} fluid + {case.nbS} wall particles, dx={case.dx:.4g}, Oldroyd-B "
-                               f"Re=0.01 Wi={args.wi} beta=0.59, periodic x, {args.precision}",
+        "config": {"workload": workload_text(args, case),
                    "npfb": case.npfb, "n_fluid": n_fluid, "precision": args.precision,
                    "parallelism": f"replicas x{dist.world}",
                    "l2": "inputs larger than L2 (ELL matrix and pair arrays are several GB)"},
         "LS_iters_per_step": iters_per_step,
         "LS_residual_last": st["LS_residual"],
         "stage_ms_per_step": {abi.STAGE_NAMES[i]: round(v / args.steps, 3) for i, v in enumerate(stage) if v > 0},
+        "stage_bandwidth": stage_bandwidth({abi.STAGE_NAMES[i]: v / args.steps for i, v in enumerate(stage) if v > 0},
+                                           case.npfb, nnz_off / case.npfb, prec == abi.PREC_MIXED, peak),
         "gpu_launches": st["gpu_launches"],
         "roofline": roof,
         "e2e": e2e,
@@ -479,14 +519,18 @@ def mixed_summary(f64: dict, mx: dict) -> dict:
     us = max(np.abs(b["ux"]).max(), np.abs(b["uy"]).max())
     du = max(np.abs(a["ux"] - b["ux"]).max(), np.abs(a["uy"] - b["uy"]).max()) / us
     dp = np.abs(a["p"] - b["p"]).max() / max(np.abs(b["p"]).max(), 1e-300)
-    wake = b["rx"] > 1.0
+    wake = b["rx"] > 1.0  # behind the cylinder (centred at x = 0); the whole channel elsewhere
+    if not wake.any():
+        wake = np.ones_like(wake)
     n1a = float((a["tau11"] - a["tau22"])[wake].max())
     n1b = float((b["tau11"] - b["tau22"])[wake].max())
+    dt11 = np.abs(a["tau11"] - b["tau11"]).max() / max(np.abs(b["tau11"]).max(), 1e-300)
     return {"value": mx["value"], "unit": UNIT, "ms_per_step": mx["ms_per_step"],
             "speedup_vs_fp64": mx["value"] / f64["value"], "LS_iters_per_step": mx["LS_iters_per_step"],
             "LS_residual_last": mx["LS_residual_last"], "roofline": mx["roofline"],
             "stage_ms_per_step": mx["stage_ms_per_step"], "gpu_launches": mx["gpu_launches"],
-            "rel_diff_vs_fp64": {"u": float(du), "p": float(dp), "N1_wake_max": abs(n1a - n1b) / max(abs(n1b), 1e-300)},
+            "rel_diff_vs_fp64": {"u": float(du), "p": float(dp), "tau_xx": float(dt11),
+                                 "N1_wake_max": abs(n1a - n1b) / max(abs(n1b), 1e-300)},
             "N1_wake_max": {"mixed": n1a, "fp64": n1b},
             "drag": mx.get("drag"),
             "drag_rel_diff_vs_fp64": (abs(mx["drag"]["F_x"] - f64["drag"]["F_x"]) / abs(f64["drag"]["F_x"])
@@ -496,7 +540,7 @@ def mixed_summary(f64: dict, mx: dict) -> dict:
                      "(tests/test_gpu_mixed.py)")}
 
 
-def multigrid_summary(plain: dict, f64: dict, mx: dict) -> dict:
+def multigrid_summary(plain: dict, f64: dict, mx: dict, pert: dict | None = None) -> dict:
     """The opt-in multigrid-preconditioned PPE on the same workload: FP64 and mixed precision,
     both converging to the solver tolerance; speed-ups and the mixed-vs-FP64 differences."""
     keep = ("value", "ms_per_step", "LS_iters_per_step", "LS_residual_last", "stage_ms_per_step", "roofline",
@@ -508,6 +552,10 @@ def multigrid_summary(plain: dict, f64: dict, mx: dict) -> dict:
     d = mixed_summary(f64, mx)
     out["mixed_vs_fp64"] = {"rel_diff": d["rel_diff_vs_fp64"], "drag_rel_diff": d["drag_rel_diff_vs_fp64"],
                             "N1_wake_max": d["N1_wake_max"]}
+    if pert is not None:  # the flow's own sensitivity: FP64 from positions moved at FP32 rounding level
+        e = mixed_summary(f64, pert)
+        out["fp64_self_spread"] = {"rel_diff": e["rel_diff_vs_fp64"], "drag_rel_diff": e["drag_rel_diff_vs_fp64"],
+                                   "perturbation": "fluid positions + 6e-8 dx (seeded normal), FP64, same steps"}
     out["note"] = ("opt-in (ppe_precond = VEBI_PRECOND_MULTIGRID): aggregation multigrid on the cell grid; "
                    "both precisions converge to tol 1e-8 each step, the plain solver stops at its 1000-iteration cap")
     return out
@@ -609,11 +657,12 @@ def main():
             res["mixed"] = mixed_summary(res, mres)
         if args.precond == "none" and not args.no_multigrid and not args.batch:
             runs = []
-            for p in ("fp64", "mixed"):
+            for p, pert in (("fp64", 0.0), ("mixed", 0.0), ("fp64", 6e-8)):
                 gargs = argparse.Namespace(**vars(args))
                 gargs.precision, gargs.precond, gargs.no_e2e, gargs.no_cpu = p, "multigrid", True, True
+                gargs.perturb = pert
                 runs.append(run_gb300(gargs, dist))
-            res["multigrid"] = multigrid_summary(res, runs[0], runs[1])
+            res["multigrid"] = multigrid_summary(res, runs[0], runs[1], runs[2])
         res.pop("_fields", None)
     else:
         from oracle import build as ob
