@@ -16,6 +16,7 @@ CASES = {
     "cylinder20k": lambda: cases.cylinder(2.0e4, Wi=0.6, seed=2),
     "cavity64": lambda: cases.cavity(64, seed=3),
     "free_surface_open": lambda: cases.free_surface_periodic(75, seed=5),
+    "dam_break_open": lambda: cases.dam_break(40, seed=3),
 }
 
 
@@ -66,7 +67,7 @@ def test_multigrid_is_deterministic(libs):
     assert np.array_equal(out[0][1], out[1][1]) and np.array_equal(out[0][2], out[1][2])
 
 
-@pytest.mark.parametrize("name", ["poiseuille40", "cylinder20k", "free_surface_open"])
+@pytest.mark.parametrize("name", ["poiseuille40", "cylinder20k", "free_surface_open", "dam_break_open"])
 def test_mixed_multigrid_close_to_fp64(libs, name):
     """Mixed precision with the preconditioner against the FP64 step with it: velocity, and for
     the cylinder the drag, within 1e-4 after three steps (both solves converge)."""

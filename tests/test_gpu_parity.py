@@ -16,6 +16,7 @@ CASES = {
     "cavity64": lambda: cases.cavity(64, seed=3),
     "poiseuille_newtonian": lambda: cases.poiseuille(32, seed=4, const_mod=1),
     "free_surface_open": lambda: cases.free_surface_periodic(75, seed=5),
+    "dam_break_open": lambda: cases.dam_break(40, seed=3),
     "poiseuille_correct_velocity": lambda: _with(cases.poiseuille(40, seed=6), correct_velocity=1),
 }
 

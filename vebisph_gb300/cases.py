@@ -463,6 +463,44 @@ def free_surface_periodic(n: int = 75, seed: int | None = None) -> Case:
                 b_thermal=b_th, b_periodic_parent=np.array([0, 4, 0, 2]))
 
 
+def dam_break(m: int = 40, seed: int | None = None) -> Case:
+    """Open-domain case: datclass case 1 "2 d dam break" (datclass.F90:47-117) -- a unit box
+    with four no-slip walls, a water column x <= h0, y <= 2 h0 (h0 = 0.25) in the lower-left
+    corner, gravity body force (0, -1), i_open_domain=1, shift_coeff=0, Newtonian (beta=1,
+    El=0: const_mod 1), Ra=1e4, Pr=1, dx = h0/m (the generator's m = 40).  seed=None gives the
+    unjittered lattice of the generator."""
+    xl = yl = 1.0
+    h0 = 0.25
+    dx = h0 / m
+    h = 1.3 * dx
+    b_node = np.array([[0.0, 0.0], [xl, 0.0], [xl, yl], [0.0, yl]])
+    b_edge = make_boundary_edge_vectors(b_node)
+    b_type = np.array([1, 1, 1, 1])
+    b_vel = np.zeros(4)
+    b_th = np.zeros(4)
+    xs, ys, us, vs, ths = make_boundary_particles(b_node, b_edge, b_type, b_vel, b_th, dx)
+    fx, fy = [], []
+    x = 0.0 + dx * 0.5
+    while x < xl - 0.5 * dx:
+        y = 0.0 + dx * 0.5
+        while y < yl - 0.5 * dx:
+            if x <= h0 and y <= 2.0 * h0:
+                fx.append(x)
+                fy.append(y)
+            y = y + dx
+        x = x + dx
+    fr = np.stack([fx, fy], 1)
+    if seed is not None:
+        fr += _jitter(np.random.default_rng(seed), len(fr), dx)
+    r = np.concatenate([np.stack([xs, ys], 1), fr])
+    u = np.zeros_like(r)
+    theta = np.concatenate([ths, np.zeros(len(fr))])
+    return Case(name=f"dam_break_{m}", r=r, u=u, theta=theta, npfb=len(r), nbS=len(xs), h=h, dx=dx, dv=dx * dx,
+                Ra=1.0e4, Pr=1.0, El=0.0, beta=1.0, body_force=(0.0, -1.0), ve_nonlinearity=100.0,
+                i_open_domain=1, i_shift_coeff=0, const_mod=1, b_node=b_node, b_edge=b_edge, b_type=b_type,
+                b_vel=b_vel, b_thermal=b_th, b_periodic_parent=np.array([3, 4, 1, 2]))
+
+
 def by_name(name: str, **kw) -> Case:
     table = {
         "poiseuille_40": lambda: poiseuille(40, **kw),
