@@ -16,6 +16,7 @@
 // formatter reproduces the reference's own list-directed files byte for byte
 // (source/gen/IPART, IBOUND; tests/test_output_format.py).
 #include <algorithm>
+#include <charconv>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -42,7 +43,9 @@ static int fmt_real8(double v, char* o) {
     len = std::snprintf(num, sizeof(num), "%s0.0000000000000000     ", std::signbit(v) ? "-" : "");
   } else {
     char e[40];
-    std::snprintf(e, sizeof(e), "%.16e", std::fabs(v));  // d.dddddddddddddddde+XX, rounded
+    // d.dddddddddddddddde+XX, correctly rounded to 17 significant digits (as printf's %.16e)
+    const auto res = std::to_chars(e, e + sizeof(e) - 1, std::fabs(v), std::chars_format::scientific, 16);
+    *res.ptr = '\0';
     char dig[17];
     dig[0] = e[0];
     std::memcpy(dig + 1, e + 2, 16);
@@ -84,7 +87,7 @@ static int fmt_real8(double v, char* o) {
 // one integer(4) item: 12 characters (a blank separator and I11)
 static int fmt_int4(int v, char* o) {
   char t[24];
-  int len = std::snprintf(t, sizeof(t), "%d", v);
+  const int len = (int)(std::to_chars(t, t + sizeof(t), v).ptr - t);
   const int w = len > 11 ? len : 11;
   o[0] = ' ';
   std::memset(o + 1, ' ', (size_t)(w - len));
