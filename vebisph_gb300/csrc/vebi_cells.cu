@@ -82,7 +82,6 @@ __global__ void k_scan_top(Dev d, int nblk) {
 
 // pass 3: per-block exclusive scan plus block offset -> cell_start (ist)
 __global__ void k_scan_apply(Consts c, Dev d) {
-  __shared__ int sh[SCAN_CH];
   __shared__ int wsum[32];
   int b0 = blockIdx.x * SCAN_CH;
   // each thread owns SCAN_CH/blockDim consecutive cells
@@ -114,7 +113,6 @@ __global__ void k_scan_apply(Consts c, Dev d) {
     run += vals[q];
     if (cc == c.nct - 1) d.cell_start[c.nct] = run;
   }
-  (void)sh;
 }
 
 __global__ void k_scatter(Dev d) {
