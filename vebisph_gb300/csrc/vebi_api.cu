@@ -278,7 +278,8 @@ struct vebi_ctx {
 extern "C" {
 
 const char* vebi_version(void) {
-  return "vebisph-gb300 step library: FP64 div_free on sm_103a (ELL pair lists, persistent BiCGSTAB)";
+  return "vebisph-gb300 step library for sm_103a: the div_free step in FP64 (the reference's arithmetic) or mixed "
+         "precision, persistent BiCGSTAB with an optional multigrid preconditioner, batches, output files";
 }
 
 const char* vebi_last_error(void) { return g_err.c_str(); }
