@@ -217,6 +217,7 @@ static int allocate_all(Ctx& x) {
   A_(d.scan_part, (size_t)c.nct / 1024 + 2);
   size_t sel_items = (size_t)(c.npfb > c.mcap ? c.npfb : c.mcap);
   A_(d.sel_blk, sel_items / SEL_CH + 2);
+  A_(d.cand, n); A_(d.cand_blk, n / SEL_CH + 2);
   A_(d.pk, cap);
   A_(d.ij_count, n); A_(d.ij_link, E);
   A_(d.wGx, E); A_(d.wGy, E); A_(d.wL, E);

@@ -65,6 +65,7 @@ struct Scal {
   int warnings;
   int error;
   int sel_base;                      // mirror offset of the current ordered-select stage
+  int n_cand;                        // particles in cand (candidates of the mirror stages)
   int sel_total;
   int imp_temp;                      // mirror count snapshot for wall-periodic corners
   int bar_count;                     // grid barrier state of the PPE kernel
@@ -116,6 +117,7 @@ struct Dev {
   int *scan_part;
   // ordered select scratch
   int* sel_blk;
+  int *cand, *cand_blk;                      // particles near a boundary or circle, ascending
   // pairs
   int *ij_count, *ij_link;
   double *wGx, *wGy, *wL;

@@ -170,6 +170,7 @@ struct SelArgs {
   int ib;      // patch (0-based)
   int n0;      // first item
   int n1;      // end item (static kinds)
+  int cand;    // 1: the items are the candidate list (particles 0..npfb near a boundary), from n0
 };
 
 // near-patch test of create_boundary_boxes: |perp| <= sup+1e-10 and 0<=tmp<=1
@@ -370,14 +371,27 @@ __device__ void sel_emit(const Consts& c, const Dev& d, const SelArgs& a, int it
 }
 
 // per-block item counts
+// item q of a stage: a particle or mirror index, or -1 past the end.  In candidate mode the
+// items are the ascending candidate list, and those below n0 count nothing, so every stage
+// still visits its items in ascending index order.
+__device__ __forceinline__ int sel_item(const Consts& c, const Dev& d, const SelArgs& a, int q, int n1) {
+  if (a.cand) {
+    if (q >= d.s->n_cand) return -1;
+    const int it = d.cand[q];
+    return it >= a.n0 ? it : -1;
+  }
+  const int it = a.n0 + q;
+  return it < n1 ? it : -1;
+}
+
 __global__ void k_sel_count(Consts c, Dev d, SelArgs a) {
   __shared__ int sh[TPB / 32];
   const int n1 = sel_end(c, d, a);
-  int base = a.n0 + blockIdx.x * SEL_CH + threadIdx.x * SEL_IPT;
+  int base = blockIdx.x * SEL_CH + threadIdx.x * SEL_IPT;
   int cnt = 0;
   for (int q = 0; q < SEL_IPT; ++q) {
-    int it = base + q;
-    if (it < n1) cnt += sel_count(c, d, a, it);
+    int it = sel_item(c, d, a, base + q, n1);
+    if (it >= 0) cnt += sel_count(c, d, a, it);
   }
   for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = cnt;
@@ -426,12 +440,12 @@ __global__ void k_sel_scan(Dev d, int nblk, int mcap) {
 __global__ void k_sel_emit(Consts c, Dev d, SelArgs a) {
   __shared__ int sh[TPB / 32 + 1];
   const int n1 = sel_end(c, d, a);
-  int base = a.n0 + blockIdx.x * SEL_CH + threadIdx.x * SEL_IPT;
-  int cnts[SEL_IPT];
+  int base = blockIdx.x * SEL_CH + threadIdx.x * SEL_IPT;
+  int cnts[SEL_IPT], items[SEL_IPT];
   int tot = 0;
   for (int q = 0; q < SEL_IPT; ++q) {
-    int it = base + q;
-    cnts[q] = (it < n1) ? sel_count(c, d, a, it) : 0;
+    items[q] = sel_item(c, d, a, base + q, n1);
+    cnts[q] = items[q] >= 0 ? sel_count(c, d, a, items[q]) : 0;
     tot += cnts[q];
   }
   // block exclusive scan of tot in thread order
@@ -451,10 +465,138 @@ __global__ void k_sel_emit(Consts c, Dev d, SelArgs a) {
   int slot = d.s->sel_base + d.sel_blk[blockIdx.x] + sh[w] + inc - tot;
   for (int q = 0; q < SEL_IPT; ++q) {
     if (cnts[q]) {
-      sel_emit(c, d, a, base + q, slot);
+      sel_emit(c, d, a, items[q], slot);
       slot += cnts[q];
     }
   }
+}
+
+// The candidates of the mirror stages: particles 0..npfb within the support of a boundary line
+// or a circle.  Every item any stage over particles can select is one: a wall or periodic
+// image needs |perp| <= sup + 1e-10 to that patch's line, a corner image a node distance within
+// the same bound (the node is on both lines), a circle image rad within R + sup (or |R| - sup).
+// The test runs in FP32 with a margin of dx/10 plus 4e-6 of the box's extent, far above its
+// rounding error, so the list is a superset of every stage's selection; the stages then apply
+// their own FP64 tests.
+struct NearTab {
+  float a[VEBI_MAX_PATCHES], b[VEBI_MAX_PATCHES], c0[VEBI_MAX_PATCHES];  // perp = a x + b y + c0
+  float cx[VEBI_MAX_CIRCLES], cy[VEBI_MAX_CIRCLES], lo2[VEBI_MAX_CIRCLES], hi2[VEBI_MAX_CIRCLES];
+  float band;
+  int np, nc;
+};
+
+__device__ void near_table(const Consts& c, NearTab& t) {
+  const double ext = fmax(fmax(fabs(c.x_mint), fabs(c.x_maxt)), fmax(fabs(c.y_mint), fabs(c.y_maxt)));
+  const double m = c.sup_size + 0.1 * c.dx + 4.0e-6 * ext;
+  if (threadIdx.x == 0) {
+    int k = 0;
+    for (int ib = 0; ib < c.nb; ++ib) {
+      if (c.b_type[ib] == 0) continue;
+      const int ibp1 = (ib + 1) % c.nb;
+      const double inv = -1.0 / c.b_elen[ib];
+      t.a[k] = (float)(c.b_edge[ib][1] * inv);
+      t.b[k] = (float)(-c.b_edge[ib][0] * inv);
+      t.c0[k] = (float)((c.b_node[ibp1][0] * c.b_node[ib][1] - c.b_node[ibp1][1] * c.b_node[ib][0]) * inv);
+      ++k;
+    }
+    t.np = k;
+    for (int ic = 0; ic < c.ncirc; ++ic) {
+      const double R = c.c_radius[ic];
+      t.cx[ic] = (float)c.c_centre[ic][0];
+      t.cy[ic] = (float)c.c_centre[ic][1];
+      if (R > 0.0) { t.lo2[ic] = -1.0f; t.hi2[ic] = (float)((R + m) * (R + m)); }
+      else { const double l = fmax(fabs(R) - m, 0.0); t.lo2[ic] = (float)(l * l); t.hi2[ic] = 3.0e38f; }
+    }
+    t.nc = c.ncirc;
+    t.band = (float)m;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ bool near_boundary(const NearTab& t, double xd, double yd) {
+  const float x = (float)xd, y = (float)yd;
+  for (int k = 0; k < t.np; ++k)
+    if (fabsf(fmaf(t.a[k], x, fmaf(t.b[k], y, t.c0[k]))) <= t.band) return true;
+  for (int ic = 0; ic < t.nc; ++ic) {
+    const float r1 = x - t.cx[ic], r2 = y - t.cy[ic];
+    const float q = fmaf(r1, r1, r2 * r2);
+    if (t.lo2[ic] < 0.0f ? q <= t.hi2[ic] : q >= t.lo2[ic]) return true;
+  }
+  return false;
+}
+
+__global__ void k_cand_count(Consts c, Dev d) {
+  __shared__ int sh[TPB / 32];
+  __shared__ NearTab t;
+  near_table(c, t);
+  const int base = blockIdx.x * SEL_CH + threadIdx.x * SEL_IPT;
+  int cnt = 0;
+  for (int q = 0; q < SEL_IPT; ++q) {
+    const int it = base + q;
+    if (it < c.npfb && near_boundary(t, d.rx[it], d.ry[it])) ++cnt;
+  }
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int tt = 0;
+    for (int w = 0; w < TPB / 32; ++w) tt += sh[w];
+    d.cand_blk[blockIdx.x] = tt;
+  }
+}
+
+__global__ void k_cand_scan(Dev d, int nblk) {
+  __shared__ int sh[1024];
+  const int T = blockDim.x;
+  const int per = (nblk + T - 1) / T;
+  const int b0 = threadIdx.x * per, b1 = min(nblk, b0 + per);
+  int loc = 0;
+  for (int b = b0; b < b1; ++b) loc += d.cand_blk[b];
+  sh[threadIdx.x] = loc;
+  __syncthreads();
+  for (int o = 1; o < T; o <<= 1) {
+    int v = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+    __syncthreads();
+    sh[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int run = sh[threadIdx.x] - loc;
+  for (int b = b0; b < b1; ++b) {
+    int v = d.cand_blk[b];
+    d.cand_blk[b] = run;
+    run += v;
+  }
+  if (threadIdx.x == T - 1) d.s->n_cand = sh[T - 1];
+}
+
+__global__ void k_cand_emit(Consts c, Dev d) {
+  __shared__ int sh[TPB / 32 + 1];
+  __shared__ NearTab t;
+  near_table(c, t);
+  const int base = blockIdx.x * SEL_CH + threadIdx.x * SEL_IPT;
+  bool f[SEL_IPT];
+  int tot = 0;
+  for (int q = 0; q < SEL_IPT; ++q) {
+    const int it = base + q;
+    f[q] = it < c.npfb && near_boundary(t, d.rx[it], d.ry[it]);
+    tot += f[q] ? 1 : 0;
+  }
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int inc = tot;
+  for (int o = 1; o < 32; o <<= 1) {
+    int v = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += v;
+  }
+  if (lane == 31) sh[w] = inc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int q = 0; q < TPB / 32; ++q) { int v = sh[q]; sh[q] = run; run += v; }
+  }
+  __syncthreads();
+  int slot = d.cand_blk[blockIdx.x] + sh[w] + inc - tot;
+  for (int q = 0; q < SEL_IPT; ++q)
+    if (f[q]) d.cand[slot++] = base + q;
 }
 
 __global__ void k_snapshot_imp(Scal* s) { s->imp_temp = s->nmirror; }
@@ -476,7 +618,10 @@ __global__ void k_solid_fixup(Consts c, Dev d) {
 __global__ void k_set_np(Consts c, Scal* s) { s->np = c.npfb + s->nmirror; }
 
 static void run_stage(Ctx& x, int kind, int ib, int n0, int n1_static, int n_items_bound) {
-  SelArgs a{kind, ib, n0, n1_static};
+  // stages over particles (their items end at npfb) walk the candidate list instead
+  const int cand = n1_static == x.c.npfb ? 1 : 0;
+  SelArgs a{kind, ib, n0, n1_static, cand};
+  if (cand) n_items_bound = x.c.npfb;  // the list can hold every particle, walls included
   int nblk = (n_items_bound + SEL_CH - 1) / SEL_CH;
   if (nblk < 1) nblk = 1;
   VEBI_LAUNCH(x, k_sel_count, nblk, TPB, x.c, x.d, a);
@@ -494,6 +639,12 @@ void launch_advect_bin(Ctx& x) {
 // create_mirror_particles (mirror_boundaries_mod.F90:18-334)
 void launch_mirrors(Ctx& x) {
   const Consts& c = x.c;
+  {  // the candidate list of the stages over particles, in ascending index
+    const int nblk = (c.npfb + SEL_CH - 1) / SEL_CH;
+    VEBI_LAUNCH(x, k_cand_count, nblk, TPB, c, x.d);
+    VEBI_LAUNCH(x, k_cand_scan, 1, 1024, x.d, nblk);
+    VEBI_LAUNCH(x, k_cand_emit, nblk, TPB, c, x.d);
+  }
   if (c.ncirc > 0) run_stage(x, SEL_CIRCLES, 0, c.nbS, c.npfb, c.npfb - c.nbS);
   for (int ib = 0; ib < c.nb; ++ib) {
     if (c.b_type[ib] == 1) run_stage(x, SEL_WALL, ib, 0, c.npfb, c.npfb);
