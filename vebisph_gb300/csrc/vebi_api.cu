@@ -193,6 +193,18 @@ static int build_consts(Ctx& x) {
   c.nct = (int)nct;
   // mirror capacity: create_mirror_particles' estimate (mirror_boundaries_mod.F90:53-54)
   c.mcap = P.nmirror_cap > 0 ? P.nmirror_cap : (P.npfb <= 500 ? 10 * P.npfb : 2 * P.npfb);
+  for (int i = 0; i < nb; ++i) {  // FP32 line table of the prefilters (bound_dist's expression)
+    const int ip1 = (i + 1) % nb;
+    const double inv = -1.0 / c.b_elen[i];
+    c.bl_a[i] = (float)(c.b_edge[i][1] * inv);
+    c.bl_b[i] = (float)(-c.b_edge[i][0] * inv);
+    c.bl_c[i] = (float)((c.b_node[ip1][0] * c.b_node[i][1] - c.b_node[ip1][1] * c.b_node[i][0]) * inv);
+  }
+  {
+    const double ext = std::fmax(std::fmax(std::fabs(c.x_mint), std::fabs(c.x_maxt)),
+                                 std::fmax(std::fabs(c.y_mint), std::fabs(c.y_maxt)));
+    c.near_band = (float)(c.sup_size + 0.1 * c.dx + 4.0e-6 * ext);
+  }
   c.cap = c.npfb + c.mcap;
   return VEBI_OK;
 }

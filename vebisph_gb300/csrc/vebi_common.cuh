@@ -32,6 +32,10 @@ struct Consts {
   double b_node[VEBI_MAX_PATCHES][2], b_edge[VEBI_MAX_PATCHES][2];
   double b_vel[VEBI_MAX_PATCHES], b_thermal[VEBI_MAX_PATCHES];
   double b_elen[VEBI_MAX_PATCHES];                  // sqrt(dot(b_edge,b_edge))
+  // FP32 prefilters: bound_dist ~ bl_a x + bl_b y + bl_c; near_band = sup + dx/10 + 4e-6 x the
+  // box extent, a margin far above the FP32 rounding of that expression
+  float bl_a[VEBI_MAX_PATCHES], bl_b[VEBI_MAX_PATCHES], bl_c[VEBI_MAX_PATCHES];
+  float near_band;
   double b_corner_angle[VEBI_MAX_PATCHES];          // check_boundaries (input.F90:246-270)
   double b_rot[VEBI_MAX_PATCHES][4];                // angle_between_patches(ib, parent), row-major
   double c_centre[VEBI_MAX_CIRCLES][2], c_radius[VEBI_MAX_CIRCLES], c_omega[VEBI_MAX_CIRCLES];

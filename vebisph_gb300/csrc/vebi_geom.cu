@@ -107,8 +107,17 @@ __device__ __forceinline__ double advect_bin_one(const Consts& c, const Dev& d, 
   // replace_escapees: circles (no bin test in the reference), then walls / periodic patches
   int nesc = 0;
   bool touched = false;
+  // FP32 prefilters (margin near_band): a particle clearly away from a circle or a patch skips
+  // the FP64 tests, which would find nothing to do for it
+  const float band = c.near_band;
   for (int ic = 0; ic < c.ncirc; ++ic) {
     double R = c.c_radius[ic];
+    {  // from the current position: an earlier circle may have moved the particle
+      const float d1 = (float)x - (float)c.c_centre[ic][0], d2 = (float)y - (float)c.c_centre[ic][1];
+      const float q = fmaf(d1, d1, d2 * d2), Rf = (float)fabs(R);
+      if (R > 0.0 && q > (Rf + band) * (Rf + band)) continue;              // clearly outside
+      if (R < 0.0 && Rf > band && q < (Rf - band) * (Rf - band)) continue;  // clearly inside
+    }
     double ric1 = x - c.c_centre[ic][0], ric2 = y - c.c_centre[ic][1];
     double rad = sqrt(ric1 * ric1 + ric2 * ric2);
     if (rad < fabs(R) && R > 0.0) {
@@ -126,6 +135,10 @@ __device__ __forceinline__ double advect_bin_one(const Consts& c, const Dev& d, 
   for (int p = 0; p < c.nb; ++p) {
     if (c.b_type[p] != 1 && c.b_type[p] != 2) continue;
     if (ib) continue;
+    {
+      const float pf = fmaf(c.bl_a[p], (float)x, fmaf(c.bl_b[p], (float)y, c.bl_c[p]));
+      if (pf > band || pf < -band) continue;  // clearly inside, or clearly beyond the support
+    }
     double perp = bound_dist(c, x, y, p);
     if (perp > 0.0) continue;
     if (fabs(perp) > c.sup_size + 1.0e-10) continue;
@@ -486,17 +499,14 @@ struct NearTab {
 };
 
 __device__ void near_table(const Consts& c, NearTab& t) {
-  const double ext = fmax(fmax(fabs(c.x_mint), fabs(c.x_maxt)), fmax(fabs(c.y_mint), fabs(c.y_maxt)));
-  const double m = c.sup_size + 0.1 * c.dx + 4.0e-6 * ext;
+  const double m = c.near_band;
   if (threadIdx.x == 0) {
     int k = 0;
     for (int ib = 0; ib < c.nb; ++ib) {
       if (c.b_type[ib] == 0) continue;
-      const int ibp1 = (ib + 1) % c.nb;
-      const double inv = -1.0 / c.b_elen[ib];
-      t.a[k] = (float)(c.b_edge[ib][1] * inv);
-      t.b[k] = (float)(-c.b_edge[ib][0] * inv);
-      t.c0[k] = (float)((c.b_node[ibp1][0] * c.b_node[ib][1] - c.b_node[ibp1][1] * c.b_node[ib][0]) * inv);
+      t.a[k] = c.bl_a[ib];
+      t.b[k] = c.bl_b[ib];
+      t.c0[k] = c.bl_c[ib];
       ++k;
     }
     t.np = k;
