@@ -61,8 +61,17 @@ __device__ __forceinline__ void slot_store(const MgLevel& L, int row, const int*
 // column (its own cell first, with the diagonal) into MG_ROW_SLOTS (cell, value) pairs,
 // [t][i] layout.  Cells: one thread per cell merges its particles' pairs in ascending particle
 // order.  val32 (mixed precision) replaces the FP64 values when given.
-__global__ void k_mg_rows(Consts c, Dev d, const float* __restrict__ val32, int* __restrict__ ragg,
-                          double* __restrict__ rval, int* __restrict__ rcnt) {
+//
+// A row's columns lie in the 3x3 cells around its own, except the parents of mirrors across
+// periodic boundaries.  The nine cells own + dy*ncx + dx are summed in shared memory by direct
+// index (the key difference alone picks the slot: nine distinct keys, nine distinct slots);
+// any other cell goes to a short searched list.  Each cell's sum runs in slot order, as a
+// searched table's would; the pairs come out own cell first, then the 3x3 in key order, then
+// the list.
+__global__ void __launch_bounds__(TPB) k_mg_rows(Consts c, Dev d, const float* __restrict__ val32,
+                                                 int* __restrict__ ragg, double* __restrict__ rval,
+                                                 int* __restrict__ rcnt) {
+  __shared__ double nb9[9][TPB];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.npfb) return;
   const int own = d.cellpart[i];
@@ -70,23 +79,50 @@ __global__ void k_mg_rows(Consts c, Dev d, const float* __restrict__ val32, int*
     rcnt[i] = 0;
     return;
   }
-  int tc[MG_ROW_SLOTS];
-  double tv[MG_ROW_SLOTS];
-  tc[0] = own;
-  tv[0] = d.ppe_diag[i];
-  int m = 1;
+  double* acc = &nb9[0][threadIdx.x];  // slot q at acc[q * TPB]
+#pragma unroll
+  for (int q = 0; q < 9; ++q) acc[q * TPB] = 0.0;
+  acc[4 * TPB] = d.ppe_diag[i];
+  unsigned used = 1u << 4;
+  int tc[MG_ROW_SLOTS - 9];
+  double tv[MG_ROW_SLOTS - 9];
+  int m = 0;
   bool ok = true;
+  const int ncx = c.ncx;
   const int cnt = d.ij_count[i];
   for (int k = 0; k < cnt; ++k) {
     const int a = d.cellpart[d.ppe_col[ELL(k, i)]];
     const double v = val32 ? (double)val32[ELL(k, i)] : d.ppe_val[ELL(k, i)];
-    if (a >= 0) ok &= slot_add<MG_ROW_SLOTS>(tc, tv, m, a, v);
+    if (a < 0) continue;
+    const int del = a - own;
+    const int r = del + ncx + 1;  // row dy=-1 at 0..2, dy=0 at ncx..ncx+2, dy=+1 at 2ncx..2ncx+2
+    int q = -1;
+    if (r >= 0 && r <= 2) q = r;
+    else if (r >= ncx && r <= ncx + 2) q = 3 + r - ncx;
+    else if (r >= 2 * ncx && r <= 2 * ncx + 2) q = 6 + r - 2 * ncx;
+    if (q >= 0) {
+      acc[q * TPB] += v;
+      used |= 1u << q;
+    } else {
+      ok &= slot_add<MG_ROW_SLOTS - 9>(tc, tv, m, a, v);
+    }
   }
-  for (int t = 0; t < m; ++t) {
-    ragg[(size_t)t * c.npfb + i] = tc[t];
-    rval[(size_t)t * c.npfb + i] = tv[t];
+  int t = 0;
+  ragg[i] = own;
+  rval[i] = acc[4 * TPB];
+  ++t;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    if (q == 4 || !(used & (1u << q))) continue;
+    ragg[(size_t)t * c.npfb + i] = own + (q / 3 - 1) * ncx + (q % 3 - 1);
+    rval[(size_t)t * c.npfb + i] = acc[q * TPB];
+    ++t;
   }
-  rcnt[i] = m;
+  for (int e = 0; e < m; ++e, ++t) {
+    ragg[(size_t)t * c.npfb + i] = tc[e];
+    rval[(size_t)t * c.npfb + i] = tv[e];
+  }
+  rcnt[i] = t;
   if (!ok) d.s->mg_fail = 1;
 }
 

@@ -58,6 +58,11 @@ __global__ void k_ppe_mean(Consts c, Dev d, int nblk) {
 }
 
 // ---------------------------------------------------------------------- assembly
+// Rows without a mirror neighbour (all but a thin layer along the boundaries) hold distinct
+// columns, so one pass writes each slot once with the same value (0 + temp) the general path
+// accumulates; the first mirror neighbour sends the row to the general path, which starts over.
+// The mixed step (wL32 given) also writes the FP32 off-diagonal values and the FP64 row sums
+// diag + sum_k A_ik, in slot order, that its difference-form SpMV reads.
 __global__ void k_ppe_assemble(Consts c, Dev d, const float* __restrict__ wL32) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.npfb) return;
@@ -65,35 +70,42 @@ __global__ void k_ppe_assemble(Consts c, Dev d, const float* __restrict__ wL32) 
   if (c.open_domain == 0) B = B - d.s->rhs_mean;
   const int cnt = d.ij_count[i];
   bool any_mirror = false;
-  for (int k = 0; k < cnt; ++k) {
-    int j = d.ij_link[ELL(k, i)];
-    int col = j;
-    if (j >= c.npfb) { col = d.irel[j]; any_mirror = true; }
-    d.ppe_col[ELL(k, i)] = col;
-    d.ppe_val[ELL(k, i)] = 0.0;
-  }
   double Adiag = 0.0;
   for (int k = 0; k < cnt; ++k) {
-    int j = d.ij_link[ELL(k, i)];
-    // the mixed step assembles in FP64 from its FP32 Morris weights
-    double temp = wL32 ? -(double)wL32[ELL(k, i)] : -d.wL[ELL(k, i)];
+    const int j = d.ij_link[ELL(k, i)];
+    if (j >= c.npfb) { any_mirror = true; break; }
+    const double temp = wL32 ? -(double)wL32[ELL(k, i)] : -d.wL[ELL(k, i)];
     Adiag = Adiag - temp;
-    int colk = j;
-    bool self = false;
-    if (j >= c.npfb) {
-      colk = d.irel[j];
-      if (colk == i) self = true;
-      B = B - d.dP_mp[j] * temp;
+    d.ppe_col[ELL(k, i)] = j;
+    d.ppe_val[ELL(k, i)] = 0.0 + temp;
+  }
+  if (any_mirror) {
+    for (int k = 0; k < cnt; ++k) {
+      int j = d.ij_link[ELL(k, i)];
+      d.ppe_col[ELL(k, i)] = j >= c.npfb ? d.irel[j] : j;
+      d.ppe_val[ELL(k, i)] = 0.0;
     }
-    if (self) {
-      Adiag = Adiag + temp;
-    } else {
-      int nt = k;  // last slot holding this column
-      if (any_mirror) {
+    Adiag = 0.0;
+    for (int k = 0; k < cnt; ++k) {
+      int j = d.ij_link[ELL(k, i)];
+      // the mixed step assembles in FP64 from its FP32 Morris weights
+      double temp = wL32 ? -(double)wL32[ELL(k, i)] : -d.wL[ELL(k, i)];
+      Adiag = Adiag - temp;
+      int colk = j;
+      bool self = false;
+      if (j >= c.npfb) {
+        colk = d.irel[j];
+        if (colk == i) self = true;
+        B = B - d.dP_mp[j] * temp;
+      }
+      if (self) {
+        Adiag = Adiag + temp;
+      } else {
+        int nt = k;  // last slot holding this column
         for (int kk = cnt - 1; kk >= 0; --kk)
           if (d.ppe_col[ELL(kk, i)] == colk) { nt = kk; break; }
+        d.ppe_val[ELL(nt, i)] = d.ppe_val[ELL(nt, i)] + temp;
       }
-      d.ppe_val[ELL(nt, i)] = d.ppe_val[ELL(nt, i)] + temp;
     }
   }
   if (d.n_surf[i] != 0) Adiag = 1.0e30;
@@ -104,6 +116,16 @@ __global__ void k_ppe_assemble(Consts c, Dev d, const float* __restrict__ wL32) 
     for (int k = 0; k < cnt; ++k) d.ppe_val[ELL(k, i)] = d.ppe_val[ELL(k, i)] * ps;
   }
   d.ppe_B[i] = B;
+  if (wL32) {
+    double rs = d.ppe_diag[i];
+    for (int k = 0; k < cnt; ++k) {
+      const double v = d.ppe_val[ELL(k, i)];
+      rs += v;
+      d.ppe_val32[ELL(k, i)] = (float)v;
+    }
+    d.rowsum[i] = rs;
+    if (c.open_domain == 1) d.bM[i] = 1.0 / (d.ppe_diag[i] + 1.0e-15);
+  }
 }
 
 // ---------------------------------------------------------------------- BiCGSTAB
@@ -480,21 +502,6 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab_mixed(MxArgs a) {
   }
 }
 
-// FP32 copy of the off-diagonal values and the FP64 row sums; for the Jacobi solver 1/(M+1e-15)
-__global__ void k_matrix_mixed(Consts c, Dev d) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= c.npfb) return;
-  double rs = d.ppe_diag[i];
-  const int cnt = d.ij_count[i];
-  for (int k = 0; k < cnt; ++k) {
-    double v = d.ppe_val[ELL(k, i)];
-    rs += v;
-    d.ppe_val32[ELL(k, i)] = (float)v;
-  }
-  d.rowsum[i] = rs;
-  if (c.open_domain == 1) d.bM[i] = 1.0 / (d.ppe_diag[i] + 1.0e-15);
-}
-
 int ppe_mixed_blocks(int nsm) {
   int per = 0, per2 = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_bicgstab_mixed<true>, TPB, 0);
@@ -508,7 +515,6 @@ void launch_ppe_mg_mixed(Ctx& x);
 
 void launch_ppe_mixed_solve(Ctx& x) {
   const Consts& c = x.c;
-  VEBI_LAUNCH(x, k_matrix_mixed, grid_for(c.npfb), TPB, c, x.d);
   if (c.precond) {
     launch_ppe_mg_mixed(x);
     return;

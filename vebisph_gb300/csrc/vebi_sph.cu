@@ -471,14 +471,22 @@ __global__ void k_secondary_final(Consts c, Dev d, int nblk) {
 // feel the opposite.  Evaluated after the step from the values those stages read: the
 // start-of-step fluid velocity u0, the mirrors' creation-time velocity (ux/uy at npfb..), the
 // updated tau and the new pressure.  A diagnostic of this library; the reference has none.
+// A circle mirror lies at radius 2R - rad of a source at rad (inside the support band), so a
+// particle that has one as a neighbour (distance <= sup) is within sup of the circle: the
+// mirror stages' candidate list (every particle within sup plus a margin of a boundary, in
+// ascending index) holds all of them, and the kernel walks that list alone.
+constexpr int CF_BLOCKS = 256;
+
 template <class W>
 __global__ void k_circle_force(Consts c, Dev d, const W* __restrict__ wgx, const W* __restrict__ wgy,
                                const W* __restrict__ wl_, const W* __restrict__ k11, const W* __restrict__ k21,
                                const W* __restrict__ k12, const W* __restrict__ k22) {
   __shared__ double sh[TPB / 32 + 1];
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ncand = d.s->n_cand;
   double fx = 0.0, fy = 0.0;
-  if (i >= c.nbS && i < c.npfb && !d.inbin[i]) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < ncand; q += gridDim.x * blockDim.x) {
+    const int i = d.cand[q];
+    if (i < c.nbS || i >= c.npfb || d.inbin[i]) continue;
     const bool ve = c.const_mod != 1;
     const double ui = d.u0x[i], vi = d.u0y[i], pi_ = d.p[i];
     const double K11 = (double)k11[i], K21 = (double)k21[i], K12 = (double)k12[i], K22 = (double)k22[i];
@@ -507,8 +515,8 @@ __global__ void k_circle_force(Consts c, Dev d, const W* __restrict__ wgx, const
       b = b + temp * w2;
     }
     const double gx = K11 * a + K12 * b, gy = K21 * a + K22 * b;
-    fx = c.dv * (gx - s1);
-    fy = c.dv * (gy - s2);
+    fx += c.dv * (gx - s1);
+    fy += c.dv * (gy - s2);
   }
   double bx = block_sum<TPB>(fx, sh);
   double by = block_sum<TPB>(fy, sh);
@@ -602,12 +610,12 @@ void launch_final(Ctx& x, int secondary) {
   }
   if (c.ncirc > 0) {
     if (mixed)
-      VEBI_LAUNCH(x, k_circle_force<float>, g, TPB, c, x.d, x.d.wGx32, x.d.wGy32, x.d.wL32, x.d.kgcm32[0],
+      VEBI_LAUNCH(x, k_circle_force<float>, CF_BLOCKS, TPB, c, x.d, x.d.wGx32, x.d.wGy32, x.d.wL32, x.d.kgcm32[0],
                   x.d.kgcm32[1], x.d.kgcm32[2], x.d.kgcm32[3]);
     else
-      VEBI_LAUNCH(x, k_circle_force<double>, g, TPB, c, x.d, x.d.wGx, x.d.wGy, x.d.wL, x.d.kgcm[0], x.d.kgcm[1],
+      VEBI_LAUNCH(x, k_circle_force<double>, CF_BLOCKS, TPB, c, x.d, x.d.wGx, x.d.wGy, x.d.wL, x.d.kgcm[0], x.d.kgcm[1],
                   x.d.kgcm[2], x.d.kgcm[3]);
-    VEBI_LAUNCH(x, k_circle_force_final, 1, TPB, x.d, g);
+    VEBI_LAUNCH(x, k_circle_force_final, 1, TPB, x.d, CF_BLOCKS);
   }
   if (secondary) {
     stage_mark(x, 13);
