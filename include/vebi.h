@@ -271,6 +271,40 @@ const char* vebi_version(void);
 /* Last error message of this thread (static storage). */
 const char* vebi_last_error(void);
 
+/* ---- Adjoint (reverse mode) of the step over a window --------------------------------
+ * No counterpart in the reference, which has no adjoint.  The differentiated map advances the
+ * fields (u, theta, tau) over nsteps steps with every step's geometry -- the advected positions
+ * r* at which mirrors, pair list, kernel weights, correction matrices and PPE matrix are built,
+ * and dt -- taken from the recorded base trajectory.
+ *
+ * vebi_adjoint_record runs nsteps ordinary steps from the context's state, keeping every step's
+ * geometry and the fields every checkpoint_every steps.  vebi_adjoint_replay runs the
+ * differentiated map itself from the context's current fields (upload a perturbed state first:
+ * finite differences go through it); replaying the unperturbed state reproduces the record.
+ * vebi_adjoint_restore puts a checkpointed state back into the context.  vebi_adjoint_reverse
+ * takes dJ/d(state after the window) -- seed_u (2 planes), seed_theta, seed_tau (4 planes),
+ * leading dimension ld, any of them NULL for zero -- and returns dJ/d(state before the window)
+ * in the same layout, dJ/dWi (Ra, Pr, beta fixed), and the transposed BiCGSTAB iterations.
+ * It replays each segment from its checkpoint to rebuild the steps' intermediates, so it leaves
+ * the context's fields at an intermediate state.
+ *
+ * Scope: closed domains with wall and periodic patches (and their corners), Newtonian or
+ * Oldroyd-B (ve_nonlinearity = 0), no circles, FP64 contexts, no PPE warm start, no
+ * correct_velocity; other contexts get VEBI_ERR_ARG from vebi_adjoint_create. */
+typedef struct vebi_adjoint vebi_adjoint;
+/* Set the Weissenberg number of a context (El = Wi sqrt(Pr/Ra), Ra, Pr, beta unchanged): the
+ * relaxation time of the log-conformation update and the polymeric coefficient
+ * (1-beta)/(Re Wi).  For parameter continuation and for checking dJ/dWi. */
+int vebi_set_weissenberg(vebi_ctx* ctx, double wi);
+int vebi_adjoint_create(vebi_ctx* ctx, int32_t max_steps, int32_t checkpoint_every, vebi_adjoint** out);
+int vebi_adjoint_record(vebi_adjoint* adj, int32_t nsteps, vebi_step_stats* last);
+int vebi_adjoint_replay(vebi_adjoint* adj, int32_t nsteps, vebi_step_stats* last);
+int vebi_adjoint_restore(vebi_adjoint* adj, int32_t step);
+int vebi_adjoint_reverse(vebi_adjoint* adj, const double* seed_u, const double* seed_theta, const double* seed_tau,
+                         int32_t ld, double* grad_u, double* grad_theta, double* grad_tau, double* grad_wi,
+                         int32_t* ls_iters);
+int vebi_adjoint_destroy(vebi_adjoint* adj);
+
 #ifdef __cplusplus
 }
 #endif

@@ -110,6 +110,8 @@ EXPORTED_SYMBOLS = [
     "vebi_debug_get", "vebi_version", "vebi_last_error", "vebi_ppe_solve_noalloc",
     "vebi_batch_create", "vebi_batch_get", "vebi_batch_step", "vebi_batch_destroy", "vebi_set_solver_grid",
     "vebi_dump_async", "vebi_dump_write", "vebi_dump_wait", "vebi_format_list",
+    "vebi_set_weissenberg", "vebi_adjoint_create", "vebi_adjoint_record", "vebi_adjoint_replay",
+    "vebi_adjoint_restore", "vebi_adjoint_reverse", "vebi_adjoint_destroy",
 ]
 DUMP_BACKGROUND = 1
 DUMP_RESTART_READABLE = 2
@@ -163,6 +165,18 @@ def load_library():
     lib.vebi_dump_wait.argtypes = [vp]
     lib.vebi_format_list.argtypes = [C.c_char_p, P(C.c_double), P(C.c_int32), C.c_char_p, C.c_int64]
     lib.vebi_format_list.restype = C.c_int64
+    lib.vebi_set_weissenberg.argtypes = [vp, C.c_double]
+    lib.vebi_adjoint_create.argtypes = [vp, C.c_int32, C.c_int32, P(vp)]
+    lib.vebi_adjoint_record.argtypes = [vp, C.c_int32, P(VebiStepStats)]
+    lib.vebi_adjoint_replay.argtypes = [vp, C.c_int32, P(VebiStepStats)]
+    lib.vebi_adjoint_restore.argtypes = [vp, C.c_int32]
+    lib.vebi_adjoint_reverse.argtypes = [vp, P(C.c_double), P(C.c_double), P(C.c_double), C.c_int32,
+                                         P(C.c_double), P(C.c_double), P(C.c_double), P(C.c_double),
+                                         P(C.c_int32)]
+    lib.vebi_adjoint_destroy.argtypes = [vp]
+    for fn in ("vebi_set_weissenberg", "vebi_adjoint_create", "vebi_adjoint_record", "vebi_adjoint_replay",
+               "vebi_adjoint_restore", "vebi_adjoint_reverse", "vebi_adjoint_destroy"):
+        getattr(lib, fn).restype = C.c_int
     for fn in ("vebi_batch_create", "vebi_batch_get", "vebi_batch_step", "vebi_batch_destroy", "vebi_set_solver_grid"):
         getattr(lib, fn).restype = C.c_int
     lib.vebi_version.restype = C.c_char_p

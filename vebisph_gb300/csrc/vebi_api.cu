@@ -288,6 +288,10 @@ struct vebi_ctx {
   Ctx x;
 };
 
+namespace vebi {
+Ctx* ctx_of(vebi_ctx* h) { return h ? &h->x : nullptr; }
+}  // namespace vebi
+
 extern "C" {
 
 const char* vebi_version(void) {
@@ -418,6 +422,20 @@ static void enqueue_step(Ctx& x, int secondary) {
   for (int q = 0; q < VEBI_NSTAGES; ++q) x.ev_used[q] = false;
   stage_mark(x, 0);
   launch_advect_bin(x);
+  if (x.rec_geo || x.rep_geo) {
+    const size_t B = sizeof(double) * (size_t)x.c.npfb;
+    const size_t n = (size_t)x.c.npfb;
+    if (x.rep_geo) {
+      cudaMemcpyAsync(x.d.rx, x.rep_geo, B, cudaMemcpyDeviceToDevice, x.st);
+      cudaMemcpyAsync(x.d.ry, x.rep_geo + n, B, cudaMemcpyDeviceToDevice, x.st);
+      cudaMemcpyAsync(&x.d.s->dt, x.rep_geo + 2 * n, sizeof(double), cudaMemcpyDeviceToDevice, x.st);
+    }
+    if (x.rec_geo) {
+      cudaMemcpyAsync(x.rec_geo, x.d.rx, B, cudaMemcpyDeviceToDevice, x.st);
+      cudaMemcpyAsync(x.rec_geo + n, x.d.ry, B, cudaMemcpyDeviceToDevice, x.st);
+      cudaMemcpyAsync(x.rec_geo + 2 * n, &x.d.s->dt, sizeof(double), cudaMemcpyDeviceToDevice, x.st);
+    }
+  }
   stage_mark(x, 1);
   launch_mirrors(x);
   stage_mark(x, 2);
@@ -603,6 +621,24 @@ int vebi_set_solver_grid(vebi_ctx* h, int32_t rows_per_thread) {
   x.solver_rows_per_thread = rows_per_thread;
   ++x.grid_gen;
   for (int m = 0; m < 2; ++m) {  // the captured steps hold the old grid
+    if (x.graph[m]) cudaGraphExecDestroy(x.graph[m]);
+    x.graph[m] = nullptr;
+    x.graph_failed[m] = false;
+  }
+  return VEBI_OK;
+}
+
+int vebi_set_weissenberg(vebi_ctx* h, double wi) {
+  if (!h || !(wi > 0.0)) return fail(VEBI_ERR_ARG, "bad argument");
+  Ctx& x = h->x;
+  cudaStreamSynchronize(x.st);
+  vebi_params& P = x.prm;
+  P.El = wi / std::sqrt(P.Ra / P.Pr);
+  x.c.El = P.El;
+  x.c.Wi = P.El * std::sqrt(P.Ra / P.Pr);
+  x.c.coeff_polymeric = (1.0 - P.beta) * P.Pr / (P.Ra * P.El);
+  ++x.grid_gen;
+  for (int m = 0; m < 2; ++m) {  // the captured steps hold the old constants
     if (x.graph[m]) cudaGraphExecDestroy(x.graph[m]);
     x.graph[m] = nullptr;
     x.graph_failed[m] = false;
@@ -906,3 +942,12 @@ int vebi_debug_get(vebi_ctx* h, const char* name, void* out, int64_t bytes) {
 }
 
 }  // extern "C"
+
+namespace vebi {
+int run_one_step(Ctx& x, vebi_step_stats* stats) {
+  x.launches = 0;
+  enqueue_step(x, 0);
+  if (x.timing) cudaEventRecord(x.ev[VEBI_NSTAGES], x.st);
+  return finish_step(x, stats, true);
+}
+}  // namespace vebi

@@ -46,8 +46,18 @@ struct Ctx {
   double* mg_rval = nullptr;
   std::vector<void*> allocs;
   DumpState* dump = nullptr;       // output staging (vebi_output.cu), made at the first dump
+  // adjoint window (vebi_adjoint.cu): right after advection a step records its geometry --
+  // the advected positions r* (x plane, y plane, npfb each) and dt -- into rec_geo, or takes
+  // them from rep_geo instead of its own, so that it replays a recorded step's geometry
+  double* rec_geo = nullptr;
+  const double* rep_geo = nullptr;
   vebi_step_stats last{};
 };
+
+// one step kernel by kernel (no graph), with the adjoint hooks above; the step's status
+int run_one_step(Ctx& x, vebi_step_stats* stats);
+// the context behind a handle (nullptr for a null handle)
+Ctx* ctx_of(vebi_ctx* h);
 
 // kernel launch with launch accounting and an immediate launch-error check
 #define VEBI_LAUNCH(x, kern, grid, block, ...)                         \

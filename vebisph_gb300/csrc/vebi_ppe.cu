@@ -343,6 +343,26 @@ void launch_ppe(Ctx& x) {
   x.launches++;
 }
 
+// The persistent FP64 BiCGSTAB on a caller's system (the adjoint's transposed PPE): the same
+// grid and kernels as the step's solve, other arrays.
+void launch_bicgstab_on(Ctx& x, const BiArgs& a, bool nonull) {
+  int nblk = x.coop_blocks;
+  const long long need = (a.n + TPB - 1) / TPB;
+  if (need < nblk) nblk = (int)(need < 1 ? 1 : need);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nblk);
+  cfg.blockDim = dim3(TPB);
+  cfg.stream = x.st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (nonull) cudaLaunchKernelEx(&cfg, k_bicgstab<true>, a);
+  else cudaLaunchKernelEx(&cfg, k_bicgstab<false>, a);
+  x.launches++;
+}
+
 }  // namespace vebi
 
 // =====================================================================================

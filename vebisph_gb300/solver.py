@@ -151,6 +151,68 @@ class StepSolver:
             pass
 
 
+    def set_weissenberg(self, wi: float):
+        self._check(self.lib.vebi_set_weissenberg(self.h, wi), "vebi_set_weissenberg")
+
+
+class Adjoint:
+    """Reverse mode of a StepSolver's steps over a window (vebi_adjoint_*).
+
+    record(n) runs n ordinary steps from the solver's state and keeps their geometry (advected
+    positions, dt) and the fields every `checkpoint_every` steps; replay(n) runs the
+    differentiated map -- the same steps with the recorded geometry -- from the solver's current
+    fields; reverse(...) returns dJ/d(state before the window) from dJ/d(state after it)."""
+
+    def __init__(self, solver: StepSolver, max_steps: int, checkpoint_every: int = 20):
+        self.solver = solver
+        self.lib = solver.lib
+        h = C.c_void_p()
+        solver._check(self.lib.vebi_adjoint_create(solver.h, max_steps, checkpoint_every, C.byref(h)),
+                      "vebi_adjoint_create")
+        self.h = h
+
+    def record(self, nsteps: int) -> dict:
+        s = abi.VebiStepStats()
+        self.solver._check(self.lib.vebi_adjoint_record(self.h, nsteps, C.byref(s)), "vebi_adjoint_record")
+        return s.as_dict()
+
+    def replay(self, nsteps: int) -> dict:
+        s = abi.VebiStepStats()
+        self.solver._check(self.lib.vebi_adjoint_replay(self.h, nsteps, C.byref(s)), "vebi_adjoint_replay")
+        return s.as_dict()
+
+    def restore(self, step: int = 0):
+        self.solver._check(self.lib.vebi_adjoint_restore(self.h, step), "vebi_adjoint_restore")
+
+    def reverse(self, seed_u=None, seed_theta=None, seed_tau=None) -> dict:
+        """Seeds: dJ/du (2, n), dJ/dtheta (n,), dJ/dtau (4, n) of the state after the window;
+        returns the same of the state before it, dJ/dWi and the transposed solves' iterations."""
+        n = self.solver.case.npfb
+
+        def arr(a, shape):
+            return None if a is None else np.ascontiguousarray(np.broadcast_to(a, shape), dtype=np.float64)
+
+        su, sth, sta = arr(seed_u, (2, n)), arr(seed_theta, (n,)), arr(seed_tau, (4, n))
+        gu, gth, gta = np.zeros((2, n)), np.zeros(n), np.zeros((4, n))
+        gwi = C.c_double(0.0)
+        its = C.c_int32(0)
+        self.solver._check(self.lib.vebi_adjoint_reverse(self.h, _dp(su), _dp(sth), _dp(sta), n, _dp(gu), _dp(gth),
+                                                         _dp(gta), C.byref(gwi), C.byref(its)),
+                           "vebi_adjoint_reverse")
+        return dict(u=gu, theta=gth, tau=gta, wi=gwi.value, ls_iters=its.value)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.vebi_adjoint_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class BatchSolver:
     """Independent simulations of uneven sizes advanced together (vebi_batch_*): every batch
     step replays each instance's captured step graph on its own stream; one wait per call."""
