@@ -358,6 +358,79 @@ def run_gb300(args, dist: Dist):
     return res
 
 
+def run_adjoint(args, dist: Dist) -> dict:
+    """Reverse mode on the heated-cavity workload (differentially heated square cavity,
+    args.adjoint_side^2 fluid particles, Ra=1e5, Pr=1, Oldroyd-B Wi=0.5, beta=0.5, seeded
+    perturbed temperature), FP64 step with the reference's PPE solver: J = mean kinetic energy
+    after a window of args.adjoint steps, dJ/dtheta0 (full field) and dJ/dWi, checkpoints every
+    args.checkpoint steps.  Forward cost = the plain steps of the window (captured graph);
+    adjoint cost = the reverse sweep, its recompute of every segment included.  With
+    args.adjoint_fd > 0, that many seeded directions are checked by central differences of the
+    replayed window."""
+    from vebisph_gb300 import abi, cases
+    from vebisph_gb300.solver import Adjoint, StepSolver
+    if dist.rank != 0:
+        return None
+    side, N, K = args.adjoint_side, args.adjoint, args.checkpoint
+    case = cases.cavity(n=side, seed=args.seed, Ra=1.0e5, Pr=1.0, Wi=0.5, beta=0.5)
+    case.const_mod = args.adjoint_const_mod
+    case.tol = args.adjoint_tol
+    if args.precond == "multigrid":
+        case.ppe_precond = abi.PRECOND_MULTIGRID
+    s = StepSolver(case)
+    for _ in range(max(args.warmup, args.adjoint_spinup)):
+        s.step()
+    st0 = s.download()
+    t0 = time.perf_counter()
+    _, sf = s.run_steps(N)
+    t_fwd = time.perf_counter() - t0
+    fwd_iters = sf["LS_iters_total"]
+    s.upload(st0["r"], st0["u"], st0["tau"], st0["theta"], st0["trace_conf"], st0["inbin"], case.npfb)
+    adj = Adjoint(s, max_steps=N, checkpoint_every=K)
+    t0 = time.perf_counter()
+    adj.record(N)
+    t_rec = time.perf_counter() - t0
+    fin = s.download()
+    nbS, n = case.nbS, case.npfb
+    J = 0.5 * float(np.mean(fin["u"][0, nbS:] ** 2 + fin["u"][1, nbS:] ** 2))
+    seed = np.zeros((2, n))
+    seed[:, nbS:] = fin["u"][:, nbS:] / (n - nbS)
+    t0 = time.perf_counter()
+    g = adj.reverse(seed_u=seed)
+    t_rev = time.perf_counter() - t0
+    fd = []
+    for k in range(args.adjoint_fd):
+        rng = np.random.default_rng(1000 + k)
+        d = np.zeros(n)
+        d[nbS:] = rng.normal(size=n - nbS)
+        d /= np.abs(d).max()
+        eps = 1.0e-3
+        js = []
+        for sgn in (1.0, -1.0):
+            s.upload(st0["r"], st0["u"], st0["tau"], st0["theta"] + sgn * eps * d, st0["trace_conf"], st0["inbin"], n)
+            adj.replay(N)
+            u = s.download()["u"]
+            js.append(0.5 * float(np.mean(u[0, nbS:] ** 2 + u[1, nbS:] ** 2)))
+        f = (js[0] - js[1]) / (2 * eps)
+        a = float(g["theta"] @ d)
+        fd.append({"fd": f, "adjoint": a, "rel_err": abs(f - a) / max(abs(f), 1e-300)})
+    adj.close()
+    s.close()
+    solver = ("the multigrid-preconditioned PPE (forward and transposed)" if args.precond == "multigrid"
+              else "the reference's PPE solver")
+    model = "Oldroyd-B Wi=0.5 beta=0.5" if case.const_mod != 1 else "Newtonian (const_mod 1) beta=0.5"
+    return {"workload": f"{case.name}: heated cavity, {n - nbS} fluid + {nbS} wall particles, Ra=1e5 Pr=1 "
+                        f"{model}, FP64 step, {solver}, PPE tol {case.tol:g}, {args.adjoint_spinup} steps "
+                        f"of spin-up",
+            "window_steps": N, "checkpoint_every": K, "J": J,
+            "forward_ms_per_step": 1e3 * t_fwd / N, "record_ms_per_step": 1e3 * t_rec / N,
+            "reverse_ms_per_step": 1e3 * t_rev / N, "adjoint_over_forward": t_rev / t_fwd,
+            "forward_LS_iters_per_step": fwd_iters / N, "transposed_LS_iters_per_step": g["ls_iters"] / N,
+            "dJ_dWi": g["wi"], "grad_theta_max_abs": float(np.abs(g["theta"]).max()),
+            "finite_differences": fd,
+            "timing": "host wall clock around the synchronous calls (each call waits for its GPU work)"}
+
+
 def run_batch(args, dist: Dist):
     """The batched parameter sweep: args.batch independent Poiseuille/cylinder instances with
     log-uniform fluid counts in 4k-256k, Wi ~ U[0.1, 4], beta ~ U[0.1, 0.9] (seeded), mixed
@@ -626,6 +699,15 @@ def main():
     ap.add_argument("--tune", default="1,2,4", help="solver rows-per-thread candidates of the batch autotuner")
     ap.add_argument("--warm-start", action="store_true",
                     help="opt-in: PPE starts from the previous step's pressure (changes results)")
+    ap.add_argument("--adjoint", type=int, default=0,
+                    help="measure the reverse mode over a window of this many steps (heated cavity) instead")
+    ap.add_argument("--adjoint-side", type=int, default=1024, help="cavity lattice side of the adjoint run")
+    ap.add_argument("--checkpoint", type=int, default=20, help="adjoint checkpoint interval")
+    ap.add_argument("--adjoint-fd", type=int, default=0, help="finite-difference directions checked at scale")
+    ap.add_argument("--adjoint-tol", type=float, default=1.0e-8, help="PPE tolerance of the adjoint workload")
+    ap.add_argument("--adjoint-spinup", type=int, default=20, help="steps run before the adjoint window")
+    ap.add_argument("--adjoint-const-mod", type=int, default=2, choices=[1, 2],
+                    help="constitutive model of the adjoint workload: 2 Oldroyd-B, 1 Newtonian")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -643,6 +725,12 @@ def main():
             vis = os.environ.get("CUDA_VISIBLE_DEVICES")
             ids = vis.split(",") if vis else [str(i) for i in range(dist.world)]
             os.environ["CUDA_VISIBLE_DEVICES"] = ids[dist.local % len(ids)]
+        if args.adjoint:
+            res = run_adjoint(args, dist)
+            if dist.rank == 0:
+                print(json.dumps({"adjoint": res}))
+            dist.close()
+            return
         if args.batch:
             res = run_batch(args, dist)
         else:

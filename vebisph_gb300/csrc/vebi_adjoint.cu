@@ -47,6 +47,7 @@ namespace vebi {
 
 void vebi_set_error_text(const std::string& msg);
 void launch_bicgstab_on(Ctx& x, const BiArgs& a, bool nonull);
+void launch_ppe_mg(Ctx& x);
 
 namespace {
 
@@ -414,6 +415,20 @@ __global__ void k_adj_sub_mean(int n, const double* __restrict__ sum, const doub
                                double* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = v[i] - *sum / (double)n;
+}
+__global__ void k_adj_block_sumsq(int n, const double* __restrict__ v, double* __restrict__ part) {
+  __shared__ double sh[TPB / 32 + 1];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double x = i < n ? v[i] * v[i] : 0.0;
+  x = block_sum<TPB>(x, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = x;
+}
+// v *= 1/rms (dir > 0) or rms (dir < 0), rms = sqrt(sumsq/n); a zero vector stays zero
+__global__ void k_adj_scale(int n, const double* __restrict__ sumsq, double* __restrict__ v, int dir) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double rms = sqrt(*sumsq / (double)n);
+  v[i] = rms > 0.0 ? (dir > 0 ? v[i] / rms : v[i] * rms) : 0.0;
 }
 
 // right-hand side: q_i = b-bar_i / dt and the own-row part of u*-bar
@@ -946,13 +961,33 @@ static int vjp_step(Adjoint& A, int s, const Tape& t) {
   k_adj_push<<<g, TPB, 0, x.st>>>(c, T, t.mco, -1, a.aP, 1, a.aP, nullptr, nullptr);
   // PPE: A^T lambda = P-bar with its mean removed (P has zero mean)
   project_mean(A, a.aP, a.aP);
-  x.launches += 3;
-  {
+  // The solver's convergence test turns absolute below a first residual norm of 1e-6 (the
+  // reference's rule for its pressure); adjoint right-hand sides can be any size, so the
+  // system is solved for the right-hand side scaled to unit RMS and lambda is scaled back.
+  k_adj_block_sumsq<<<g, TPB, 0, x.st>>>(n, a.aP, a.part);
+  k_adj_final_sum<<<1, TPB, 0, x.st>>>(g, a.part, A.tmp1 + 1);
+  k_adj_scale<<<g, TPB, 0, x.st>>>(n, A.tmp1 + 1, a.aP, 1);
+  x.launches += 6;
+  if (c.precond) {
+    // the context's multigrid on A^T: the same set-up and solver read the transposed arrays
+    // (piecewise-constant aggregation: the Galerkin levels of A^T are those of A transposed)
+    Dev keep = x.d;
+    x.d.ppe_col = T.acol;
+    x.d.ppe_val = T.aval;
+    x.d.ij_count = T.acnt;
+    x.d.ppe_diag = t.pdiag;
+    x.d.ppe_B = a.aP;
+    x.d.p = a.lam;
+    launch_ppe_mg(x);
+    x.d = keep;
+  } else {
     const Dev& d = x.d;
     BiArgs b{d.bx, d.br, d.brb, d.bv, d.bp, d.bpi, d.bs, d.bsi, d.bt, d.bM, d.partials, a.lam,
              a.aP, t.pdiag, T.aval, T.acol, T.acnt, d.s, (long long)n, n, c.itermax, c.tol, 0};
     launch_bicgstab_on(x, b, true);
   }
+  k_adj_scale<<<g, TPB, 0, x.st>>>(n, A.tmp1 + 1, a.lam, -1);
+  x.launches++;
   project_mean(A, a.lam, a.lam);
   // right-hand side (mean removal's adjoint is the projection above)
   k_adj_rhs_rows<<<g, TPB, 0, x.st>>>(c, t, a);

@@ -120,6 +120,22 @@ __device__ __forceinline__ M2T<T> trT(const M2T<T>& A) {
   return M2T<T>{A.a11, A.a21, A.a12, A.a22};
 }
 
+// The a21 == 0 branch below sets R = I, the limit of the general branch as a21 -> 0 (for
+// a11 != a22 the eigenvector of L1 = a11 turns by a21 / (a11 - a22)).  Its values are those of
+// the continuous map A -> R f(Lambda) R^T, but a literal derivative of the branch would drop
+// that turn; the dual carrier adds it to R's off-diagonal entries.
+__device__ __forceinline__ void diag_branch_turn(M2T<double>&, const M2T<double>&) {}
+__device__ __forceinline__ void diag_branch_turn(M2T<Dual9>& R, const M2T<Dual9>& A) {
+  const double gap = A.a11.v - A.a22.v;
+  if (gap == 0.0) return;
+#pragma unroll
+  for (int q = 0; q < NDUAL; ++q) {
+    const double ds = A.a21.d[q] / gap;
+    R.a21.d[q] = ds;
+    R.a12.d[q] = -ds;
+  }
+}
+
 template <class T>
 __device__ __forceinline__ void eigensT(const M2T<T>& A, T& L1, T& L2, M2T<T>& R) {
   T trc = A.a11 + A.a22;
@@ -139,6 +155,7 @@ __device__ __forceinline__ void eigensT(const M2T<T>& A, T& L1, T& L2, M2T<T>& R
     L1 = A.a11;
     L2 = A.a22;
     R = M2T<T>{T(1.0), T(0.0), T(0.0), T(1.0)};
+    diag_branch_turn(R, A);
   }
 }
 
