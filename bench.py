@@ -706,6 +706,7 @@ def main():
     ap.add_argument("--adjoint-fd", type=int, default=0, help="finite-difference directions checked at scale")
     ap.add_argument("--adjoint-tol", type=float, default=1.0e-8, help="PPE tolerance of the adjoint workload")
     ap.add_argument("--adjoint-spinup", type=int, default=20, help="steps run before the adjoint window")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement of the default line")
     ap.add_argument("--adjoint-const-mod", type=int, default=2, choices=[1, 2],
                     help="constitutive model of the adjoint workload: 2 Oldroyd-B, 1 Newtonian")
     args = ap.parse_args()
@@ -751,6 +752,12 @@ def main():
                 gargs.perturb = pert
                 runs.append(run_gb300(gargs, dist))
             res["multigrid"] = multigrid_summary(res, runs[0], runs[1], runs[2])
+        if not args.no_adjoint and not args.batch and dist.rank == 0:
+            # the metric's second part: adjoint/forward cost on the heated cavity (1M)
+            aargs = argparse.Namespace(**vars(args))
+            aargs.adjoint, aargs.checkpoint, aargs.precond = 20, 5, "multigrid"
+            aargs.adjoint_tol, aargs.adjoint_fd, aargs.adjoint_const_mod = 1.0e-8, 0, 2
+            res["adjoint"] = run_adjoint(aargs, dist)
         res.pop("_fields", None)
     else:
         from oracle import build as ob
