@@ -283,7 +283,7 @@ __global__ void k_adj_scan_totals(int nb, int* __restrict__ tot) {
 }
 __global__ void k_adj_scan_apply(int n, const int* __restrict__ v, const int* __restrict__ tot,
                                  int* __restrict__ ptr) {
-  // one block per ATB entries, serial inside each warp-sized chunk is enough for these sizes
+  // one block per ATB entries: thread 0 scans the block's entries serially from its offset
   __shared__ int sh[ATB];
   const int b0 = blockIdx.x * ATB;
   for (int q = threadIdx.x; q < ATB; q += blockDim.x) sh[q] = b0 + q < n ? v[b0 + q] : 0;
