@@ -288,9 +288,10 @@ const char* vebi_last_error(void);
  * It replays each segment from its checkpoint to rebuild the steps' intermediates, so it leaves
  * the context's fields at an intermediate state.
  *
- * Scope: closed domains with wall and periodic patches (and their corners), Newtonian or
- * Oldroyd-B (ve_nonlinearity = 0), no circles, FP64 contexts, no PPE warm start, no
- * correct_velocity; other contexts get VEBI_ERR_ARG from vebi_adjoint_create. */
+ * Scope: closed domains with wall and periodic patches (and their corners) and circles,
+ * Newtonian or Oldroyd-B (ve_nonlinearity = 0), FP64 contexts, no PPE warm start, no
+ * correct_velocity; other contexts get VEBI_ERR_ARG from vebi_adjoint_create.  Destroy the
+ * adjoint before its context. */
 typedef struct vebi_adjoint vebi_adjoint;
 /* Set the Weissenberg number of a context (El = Wi sqrt(Pr/Ra), Ra, Pr, beta unchanged): the
  * relaxation time of the log-conformation update and the polymeric coefficient

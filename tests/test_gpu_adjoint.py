@@ -184,3 +184,43 @@ def test_channel_gradient_matches_central_differences(channel, field):
     ad = float(np.sum(channel["g"][field] * d))
     assert abs(fd) > 0
     assert abs(fd - ad) <= RTOL * abs(fd), (fd, ad)
+
+
+@pytest.fixture(scope="module", params=[1, 2])
+def cylinder_window(request):
+    """Confined cylinder (circle mirrors, walls, periodic patches), Newtonian and Oldroyd-B,
+    ~8k fluid particles (coarse: the radius is ~11 dx, so the circle's mirrors crowd and the
+    neighbour capacity is raised to 96), from the parabolic start after a spin-up."""
+    case = cases.cylinder(8.0e3, Wi=0.6, seed=2)
+    case.const_mod = request.param
+    case.nplink = 96
+    case.tol = 1.0e-12
+    case.itermax = 4000
+    s = StepSolver(case)
+    for _ in range(SPIN):
+        s.step()
+    st0 = s.download()
+    adj = Adjoint(s, max_steps=NSTEPS, checkpoint_every=K)
+    adj.record(NSTEPS)
+    fin = s.download()
+    nbS, n = case.nbS, case.npfb
+    seed = np.zeros((2, n))
+    seed[:, nbS:] = fin["u"][:, nbS:] / (n - nbS)
+    g = adj.reverse(seed_u=seed)
+    yield dict(case=case, s=s, adj=adj, st0=st0, J0=kinetic(fin, nbS), g=g)
+    adj.close()
+    s.close()
+
+
+def test_cylinder_velocity_gradient_matches_central_differences(cylinder_window):
+    w = cylinder_window
+    case, st0 = w["case"], w["st0"]
+    assert run_from(w) == w["J0"]
+    rng = np.random.default_rng(500)
+    d = np.zeros((2, case.npfb))
+    d[:, case.nbS:] = rng.normal(size=(2, case.npfb - case.nbS))
+    d *= np.abs(st0["u"]).max() / np.abs(d).max()
+    fd = central(w, "u", d)
+    ad = float(np.sum(w["g"]["u"] * d))
+    assert abs(fd) > 0
+    assert abs(fd - ad) <= RTOL * abs(fd), (fd, ad)

@@ -29,7 +29,7 @@
 // parents, so the reverse sweep is deterministic.
 //
 // Supported: closed domains with wall (b_type 1) and periodic (b_type 2) patches and their
-// corners, Newtonian or Oldroyd-B (ve_nonlinearity = 0), no circles, FP64 arithmetic.  The
+// corners, circles, Newtonian or Oldroyd-B (ve_nonlinearity = 0), FP64 arithmetic.  The
 // adjoint also returns dJ/dWi (El = Wi sqrt(Pr/Ra) with Ra, Pr, beta fixed): Wi enters the
 // polymeric coefficient (1-beta)/(Re Wi) and the relaxation factor exp(-dt/Wi).
 //
@@ -101,6 +101,10 @@ __device__ __forceinline__ void reflect_map(const double T[4], double n1, double
 // the linear part of k_mirror_stress for mirror j of parent i: out = map(T)
 __device__ void tau_map(const Consts& c, int vr, double pr1, double pr2, const double T[4], double out[4]) {
   for (int q = 0; q < 4; ++q) out[q] = 0.0;
+  if (vr > 999) {  // circle: reflection about the radial direction
+    double nn = sqrt(pr1 * pr1 + pr2 * pr2);
+    reflect_map(T, pr1 / nn, pr2 / nn, out);
+  }
   if (vr > 0 && vr < 999) {
     int ib = vr - 1;
     if (c.b_type[ib] == 1) {
@@ -125,8 +129,9 @@ __device__ void tau_map(const Consts& c, int vr, double pr1, double pr2, const d
 }
 
 // Per-mirror coefficients of the step just run: the creation values' and the mirror
-// velocities' factor on the parent's value (sel_emit / k_mirror_velocities: 2 b - x is -1,
-// copies +1, a wall-periodic corner mirror -1 of its periodic image), and the stress map.
+// velocities' factor on the parent's value (sel_emit / k_mirror_velocities: 2 b - x is -1 for
+// walls and circles, copies +1, a wall-periodic corner mirror -1 of its periodic image), and
+// the stress map.
 // geo = the step's r* (parent positions at the mirror stages); mirrors keep theirs in d.rx.
 __global__ void k_adj_mirror_coefs(Consts c, Dev d, const double* __restrict__ geo, double* __restrict__ mco,
                                    int* __restrict__ irel_out) {
@@ -134,7 +139,11 @@ __global__ void k_adj_mirror_coefs(Consts c, Dev d, const double* __restrict__ g
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nm; m += gridDim.x * blockDim.x) {
     const int j = c.npfb + m, i = d.irel[j], vr = d.vrel[j];
     double cu = 0.0, cth = 0.0, cv = 0.0;
-    if (vr > 0 && vr < 999) {
+    if (vr > 999) {  // circle: 2 c_vel + rotation - u, 2 c_thermal - theta
+      cu = -1.0;
+      cth = -1.0;
+      cv = -1.0;
+    } else if (vr > 0 && vr < 999) {
       const int ib = vr - 1;
       if (c.b_type[ib] == 1) { cu = -1.0; cth = -1.0; cv = -1.0; }
       else if (c.b_type[ib] == 2) { cu = 1.0; cth = 1.0; cv = 1.0; }
@@ -690,7 +699,6 @@ static constexpr int CK_PLANES = 10;
 int adjoint_check_scope(const Ctx& x) {
   const Consts& c = x.c;
   if (c.open_domain) return afail(VEBI_ERR_ARG, "adjoint: closed domains only");
-  if (c.ncirc) return afail(VEBI_ERR_ARG, "adjoint: circles are not supported");
   for (int p = 0; p < c.nb; ++p)
     if (c.b_type[p] != 1 && c.b_type[p] != 2) return afail(VEBI_ERR_ARG, "adjoint: wall and periodic patches only");
   if (c.const_mod != 1 && c.eps_ptt != 0.0) return afail(VEBI_ERR_ARG, "adjoint: Oldroyd-B (ve_nonlinearity = 0) only");
