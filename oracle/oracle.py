@@ -38,6 +38,18 @@ def load():
         lib.orc_kernel_fac.restype = C.c_double
         lib.orc_eigens.argtypes = [P(C.c_double), P(C.c_double), P(C.c_double)]
         lib.orc_threads.restype = C.c_int
+        lib.orc_geometry.argtypes = [vp, C.c_int]
+        lib.orc_tlm_create.argtypes = [P(abi.VebiParams), P(C.c_int)]
+        lib.orc_tlm_create.restype = vp
+        lib.orc_tlm_destroy.argtypes = [vp]
+        lib.orc_tlm_set_state.argtypes = lib.orc_set_state.argtypes
+        lib.orc_tlm_set_tangent.argtypes = [vp, P(C.c_double), P(C.c_double), P(C.c_double), C.c_int]
+        lib.orc_tlm_step.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double,
+                                     P(abi.VebiStepStats), P(C.c_int)]
+        lib.orc_tlm_size.argtypes = [vp, C.c_char_p, P(C.c_int64)]
+        lib.orc_tlm_get.argtypes = [vp, C.c_char_p, P(C.c_double), P(C.c_double), C.c_int64]
+        lib.orc_tlm_set_itermax.argtypes = [vp, C.c_int]
+        lib.orc_tlm_box.argtypes = [vp, P(C.c_double)]
         _lib = lib
     return _lib
 
@@ -95,6 +107,24 @@ class OracleSolver:
     def set_itermax(self, itermax: int):
         self.lib.orc_set_itermax(self.h, int(itermax))
 
+    def record_geometry(self):
+        """Keep r* (after binning) and dt of every following step."""
+        self.lib.orc_geometry(self.h, 1)
+
+    def replay_geometry(self):
+        """Following steps take r* and dt from the record, from its first step on, so that a
+        rerun from perturbed fields is the map the tangent-linear model differentiates."""
+        self.lib.orc_geometry(self.h, 2)
+
+    def state(self) -> dict:
+        """The step's state in the host's Fortran planes (fluid and wall particles)."""
+        n = self.case.npfb
+        r = np.stack([self.get("rx")[:n], self.get("ry")[:n]])
+        u = np.stack([self.get("ux")[:n], self.get("uy")[:n]])
+        tau = np.stack([self.get(f"tau{c}")[:n] for c in ("11", "21", "12", "22")])
+        return dict(r=r, u=u, tau=tau, theta=self.get("theta")[:n].copy(),
+                    trace_conf=self.get("trace_conf")[:n].copy(), p=self.get("p")[:n].copy())
+
     def W(self, q: float) -> float:
         return self.lib.orc_kernel_w(self.h, q)
 
@@ -104,6 +134,89 @@ class OracleSolver:
     def close(self):
         if self.h:
             self.lib.orc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class TangentLinear:
+    """FP64 tangent-linear model of the step: the oracle run over forward-mode dual numbers.
+
+    Each field (u, theta, tau, and all computed from them) carries its derivative along one
+    direction; positions, dt, pair lists, weights and the PPE matrix are those of the
+    unperturbed trajectory, so n steps give d(state after)/d(state before) . direction of the
+    map with the geometry held at the base trajectory's."""
+
+    def __init__(self, case, state: dict | None = None):
+        self.lib = load()
+        self.case = case
+        self.params = case.params(abi.PREC_FP64)
+        st = C.c_int(0)
+        self.h = self.lib.orc_tlm_create(C.byref(self.params), C.byref(st))
+        if not self.h:
+            raise RuntimeError(f"oracle create failed: {abi.STATUS_NAMES.get(st.value, st.value)}")
+        box = (C.c_double * 4)()
+        self.lib.orc_tlm_box(self.h, box)
+        self.box = tuple(box)  # x_mint, x_maxt, y_mint, y_maxt
+        f = case.fortran_planes()
+        self.ld = f["ld"]
+        s = state or {}
+        self.upload(s.get("r", f["r"]), s.get("u", f["u"]), s.get("tau", f["tau"]),
+                    s.get("theta", f["theta"]), s.get("trace_conf", f["trace_conf"]), f["inbin"], f["ld"])
+        self.tangent_iters = 0
+
+    def upload(self, r, u, tau, theta, trace_conf, inbin, ld):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (r, u, tau, theta, trace_conf)]
+        ib = np.ascontiguousarray(inbin, dtype=np.uint8)
+        st = self.lib.orc_tlm_set_state(self.h, *[_dp(a) for a in arrs],
+                                        ib.ctypes.data_as(C.POINTER(C.c_uint8)), ld)
+        if st:
+            raise RuntimeError(f"oracle set_state: {abi.STATUS_NAMES.get(st, st)}")
+
+    def set_direction(self, du=None, dtau=None, dtheta=None):
+        """The perturbation's direction, in the host's planes; a missing field is not perturbed."""
+        n, ld = self.case.npfb, self.ld
+
+        def planes(a, k):
+            if a is None:
+                return None
+            out = np.zeros((k, ld)) if k > 1 else np.zeros(ld)
+            out[..., :n] = a
+            return np.ascontiguousarray(out)
+
+        du, dtau, dtheta = planes(du, 2), planes(dtau, 4), planes(dtheta, 1)
+        st = self.lib.orc_tlm_set_tangent(self.h, _dp(du), _dp(dtau), _dp(dtheta), ld)
+        if st:
+            raise RuntimeError(f"oracle set_tangent: {abi.STATUS_NAMES.get(st, st)}")
+
+    def step(self) -> dict:
+        s = abi.VebiStepStats()
+        it = C.c_int(0)
+        x0, x1, y0, y1 = self.box
+        st = self.lib.orc_tlm_step(self.h, x0, y0, x1, y1, C.byref(s), C.byref(it))
+        if st:
+            raise RuntimeError(f"oracle step: {abi.STATUS_NAMES.get(st, st)}")
+        self.tangent_iters = it.value
+        d = s.as_dict()
+        d["tangent_iters"] = it.value
+        return d
+
+    def get(self, name: str):
+        """(value, derivative) of a field over all particles and mirrors."""
+        n = C.c_int64()
+        if self.lib.orc_tlm_size(self.h, name.encode(), C.byref(n)):
+            raise KeyError(name)
+        v, d = np.empty(n.value), np.empty(n.value)
+        self.lib.orc_tlm_get(self.h, name.encode(), _dp(v), _dp(d), n.value)
+        return v, d
+
+    def close(self):
+        if self.h:
+            self.lib.orc_tlm_destroy(self.h)
             self.h = None
 
     def __del__(self):

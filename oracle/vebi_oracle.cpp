@@ -36,6 +36,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -50,36 +51,99 @@ inline double pw2(double x) { return x * x; }
 inline double pw4(double x) { double x2 = x * x; return x2 * x2; }
 inline double pw5(double x) { double x2 = x * x; double x3 = x * x2; return x2 * x3; }
 
-struct M2 { double a11, a12, a21, a22; };  // 2x2 matrix, Fortran (row,col)
-inline M2 mm(const M2& A, const M2& B) {    // matmul, inner index ascending
-  M2 C;
-  C.a11 = A.a11 * B.a11 + A.a12 * B.a21;
-  C.a12 = A.a11 * B.a12 + A.a12 * B.a22;
-  C.a21 = A.a21 * B.a11 + A.a22 * B.a21;
-  C.a22 = A.a21 * B.a12 + A.a22 * B.a22;
+// ---------------------------------------------------------------------- field scalar types
+// The step is written once over the scalar type R of the particle fields (u, theta, tau, P and
+// everything computed from them).  R = double is the restatement itself.  R = Tan carries one
+// directional derivative along (forward mode), which turns the same code into the FP64
+// tangent-linear model of the step: positions, dt, pair lists, kernel weights, correction
+// matrices and the PPE matrix stay plain doubles computed from the values, so the geometry of
+// every step is that of the unperturbed trajectory and only the fields are differentiated.
+struct Tan {
+  double v = 0.0, d = 0.0;
+  Tan() = default;
+  Tan(double x) : v(x), d(0.0) {}  // NOLINT: a constant carries no derivative
+  Tan(double x, double y) : v(x), d(y) {}
+};
+inline Tan operator+(const Tan& a, const Tan& b) { return Tan(a.v + b.v, a.d + b.d); }
+inline Tan operator-(const Tan& a, const Tan& b) { return Tan(a.v - b.v, a.d - b.d); }
+inline Tan operator-(const Tan& a) { return Tan(-a.v, -a.d); }
+inline Tan operator*(const Tan& a, const Tan& b) { return Tan(a.v * b.v, a.d * b.v + a.v * b.d); }
+inline Tan operator/(const Tan& a, const Tan& b) {
+  double q = a.v / b.v;
+  return Tan(q, (a.d - q * b.d) / b.v);
+}
+inline Tan operator+(const Tan& a, double b) { return Tan(a.v + b, a.d); }
+inline Tan operator+(double a, const Tan& b) { return Tan(a + b.v, b.d); }
+inline Tan operator-(const Tan& a, double b) { return Tan(a.v - b, a.d); }
+inline Tan operator-(double a, const Tan& b) { return Tan(a - b.v, -b.d); }
+inline Tan operator*(const Tan& a, double b) { return Tan(a.v * b, a.d * b); }
+inline Tan operator*(double a, const Tan& b) { return Tan(a * b.v, a * b.d); }
+inline Tan operator/(const Tan& a, double b) { return Tan(a.v / b, a.d / b); }
+inline Tan operator/(double a, const Tan& b) {
+  double q = a / b.v;
+  return Tan(q, -q * b.d / b.v);
+}
+inline Tan& operator+=(Tan& a, const Tan& b) { a = a + b; return a; }
+// branches follow the values, as the step takes them
+inline bool operator<(const Tan& a, const Tan& b) { return a.v < b.v; }
+inline bool operator>(const Tan& a, const Tan& b) { return a.v > b.v; }
+inline bool operator<=(const Tan& a, const Tan& b) { return a.v <= b.v; }
+inline bool operator>=(const Tan& a, const Tan& b) { return a.v >= b.v; }
+inline bool operator==(const Tan& a, const Tan& b) { return a.v == b.v; }
+inline bool operator!=(const Tan& a, const Tan& b) { return a.v != b.v; }
+
+inline double val(double x) { return x; }
+inline double val(const Tan& x) { return x.v; }
+inline double Sqrt(double x) { return std::sqrt(x); }
+inline double Exp(double x) { return std::exp(x); }
+inline double Log(double x) { return std::log(x); }
+// d sqrt at 0 is taken as 0: the only zero argument is the clamped eigen discriminant, a constant
+inline Tan Sqrt(const Tan& x) {
+  double s = std::sqrt(x.v);
+  return Tan(s, s > 0.0 ? 0.5 * x.d / s : 0.0);
+}
+inline Tan Exp(const Tan& x) {
+  double e = std::exp(x.v);
+  return Tan(e, e * x.d);
+}
+inline Tan Log(const Tan& x) { return Tan(std::log(x.v), x.d / x.v); }
+
+template <class T>
+struct M2T { T a11, a12, a21, a22; };  // 2x2 matrix, Fortran (row,col)
+using M2 = M2T<double>;
+template <class A, class B>
+inline auto mm(const M2T<A>& X, const M2T<B>& Y) {  // matmul, inner index ascending
+  M2T<decltype(A() * B())> C;
+  C.a11 = X.a11 * Y.a11 + X.a12 * Y.a21;
+  C.a12 = X.a11 * Y.a12 + X.a12 * Y.a22;
+  C.a21 = X.a21 * Y.a11 + X.a22 * Y.a21;
+  C.a22 = X.a21 * Y.a12 + X.a22 * Y.a22;
   return C;
 }
-inline M2 tr(const M2& A) { return M2{A.a11, A.a21, A.a12, A.a22}; }
+template <class T>
+inline M2T<T> tr(const M2T<T>& A) { return M2T<T>{A.a11, A.a21, A.a12, A.a22}; }
 
 template <class F>
-double chunk_sum(int64_t n0, int64_t n1, F f) {
+auto chunk_sum(int64_t n0, int64_t n1, F f) {
+  using S = decltype(f(n0) + 0.0);
   int64_t n = n1 - n0;
-  if (n <= 0) return 0.0;
+  if (n <= 0) return S(0.0);
   int64_t nch = (n + CHUNK - 1) / CHUNK;
-  std::vector<double> part(nch);
+  std::vector<S> part(nch);
 #pragma omp parallel for schedule(static)
   for (int64_t c = 0; c < nch; ++c) {
-    double s = 0.0;
+    S s = 0.0;
     int64_t a = n0 + c * CHUNK, b = std::min(n1, a + CHUNK);
     for (int64_t i = a; i < b; ++i) s += f(i);
     part[c] = s;
   }
-  double s = 0.0;
+  S s = 0.0;
   for (int64_t c = 0; c < nch; ++c) s += part[c];
   return s;
 }
 
-struct Oracle {
+template <class R>
+struct OracleT {
   vebi_params P{};
   // constants set by getdata (input.F90:164-172)
   double h = 0, h2 = 0, sup_size = 0, sup_size_2 = 0, uno_sup_size = 0, ad_7 = 0, ad_7h = 0,
@@ -95,7 +159,7 @@ struct Oracle {
   int n_inbin = 0, n_escapees = 0, error = 0, warnings = 0;
   double ppe_rhs_mean = 0, rms_u = 0;
   double circle_fx = 0, circle_fy = 0;     // force of the fluid on the circles (diagnostic)
-  std::vector<double> circ_s1, circ_s2;    // circle-mirror share of the predictor sums
+  std::vector<R> circ_s1, circ_s2;         // circle-mirror share of the predictor sums
   int maxneighbours = 0;
   double t_solve_ms = 0.0, t_step_ms = 0.0;  // per-step wall times (CPU baseline)
   static double wtime() {
@@ -106,24 +170,33 @@ struct Oracle {
 #endif
   }
 
-  // particle fields, capacity cap = npfb + mirror capacity
-  std::vector<double> rx, ry, ux, uy, theta, p, tau[4], trace_conf, a_out, vort, conc, div_r;
+  // particle fields (R) and geometry (double), capacity cap = npfb + mirror capacity
+  std::vector<double> rx, ry, conc, div_r;
+  std::vector<R> ux, uy, theta, p, tau[4], trace_conf, a_out, vort;
   std::vector<int> n_surf;
   std::vector<uint8_t> inbin;
   std::vector<int> irelation, vrelation;
   std::vector<double> dP_mp;
   // step temporaries kept for inspection
-  std::vector<double> r0x, r0y, u0x, u0y, rsx, rsy;  // r0/u0, and r* used for neighbours
+  std::vector<double> r0x, r0y, rsx, rsy;  // r0, and r* used for neighbours
+  std::vector<R> u0x, u0y;                 // u0
   std::vector<int> cellpart, ist, ipl, ncell;
   std::vector<int> ij_count, ij_link;  // ij_link[k*npfb+i]
   std::vector<double> wGx, wGy, wL, kgcm[4];
-  std::vector<double> grad[6];         // du/dx,du/dy,dv/dx,dv/dy,dth/dx,dth/dy over np
+  std::vector<R> grad[6];              // du/dx,du/dy,dv/dx,dv/dy,dth/dx,dth/dy over np
   std::vector<double> ushx, ushy, drx, dry, gradCx, gradCy;
-  std::vector<double> ustx, usty, thst;  // u*, theta* after the predictor (+ mirror u*)
-  std::vector<double> ppe_B, ppe_diag, ppe_val;
+  std::vector<R> ustx, usty, thst;     // u*, theta* after the predictor (+ mirror u*)
+  std::vector<R> ppe_B;
+  std::vector<double> ppe_diag, ppe_val;
   std::vector<int> ppe_col;
-  std::vector<double> gpx, gpy;
+  std::vector<R> gpx, gpy;
   std::vector<double> surf_nx, surf_ny, ppe_smooth;
+  // geometry record/replay: r* (after binning) and dt of each step, so that a rerun from
+  // perturbed fields sees the recorded geometry (the map the tangent-linear model differentiates)
+  int geo_mode = 0;  // 0 off, 1 record, 2 replay
+  size_t geo_step = 0;
+  std::vector<std::vector<double>> geo_rx, geo_ry;
+  std::vector<double> geo_dt;
 
   // ------------------------------------------------------------------ geometry helpers
   // bound_dist (mirror_boundaries_mod.F90:447-462): signed distance of a point to patch ib
@@ -267,9 +340,10 @@ struct Oracle {
     mcap = P.nmirror_cap > 0 ? P.nmirror_cap : (npfb <= 500 ? 10 * npfb : 2 * npfb);
     cap = npfb + mcap;
     auto zd = [&](std::vector<double>& v) { v.assign(cap, 0.0); };
-    zd(rx); zd(ry); zd(ux); zd(uy); zd(theta); zd(p); for (auto& t : tau) zd(t);
-    trace_conf.assign(cap, 2.0);  // input.F90:111
-    zd(a_out); zd(vort); zd(conc); zd(div_r); zd(dP_mp);
+    auto zr = [&](std::vector<R>& v) { v.assign(cap, R(0.0)); };
+    zd(rx); zd(ry); zr(ux); zr(uy); zr(theta); zr(p); for (auto& t : tau) zr(t);
+    trace_conf.assign(cap, R(2.0));  // input.F90:111
+    zr(a_out); zr(vort); zd(conc); zd(div_r); zd(dP_mp);
     n_surf.assign(cap, 0);
     inbin.assign(cap, 0);
     irelation.assign(cap, 0);
@@ -292,13 +366,29 @@ struct Oracle {
     np = npfb;
     return VEBI_OK;
   }
+  // tangent-linear model only: the direction of the fields' perturbation (any pointer may be null)
+  int set_tangent(const double* du, const double* dtp, const double* dth, int ld) {
+    if constexpr (std::is_same<R, Tan>::value) {
+      if (ld < npfb) return VEBI_ERR_ARG;
+      for (int i = 0; i < npfb; ++i) {
+        ux[i].d = du ? du[i] : 0.0;
+        uy[i].d = du ? du[ld + i] : 0.0;
+        theta[i].d = dth ? dth[i] : 0.0;
+        for (int c = 0; c < 4; ++c) tau[c][i].d = dtp ? dtp[(int64_t)c * ld + i] : 0.0;
+      }
+      return VEBI_OK;
+    } else {
+      (void)du; (void)dtp; (void)dth; (void)ld;
+      return VEBI_ERR_ARG;
+    }
+  }
 
   // ------------------------------------------------------------------ set_time_step
   // div_free.F90:126-146
   void set_time_step() {
     umax = 1.0e-10;
     for (int i = nbS; i < npfb; ++i) {
-      double u_abs = std::sqrt(ux[i] * ux[i] + uy[i] * uy[i]);
+      double u_abs = std::sqrt(val(ux[i]) * val(ux[i]) + val(uy[i]) * val(uy[i]));
       if (u_abs > umax) umax = u_abs;
     }
     double dt_CFL = P.dt_coef_cfl * h / umax;
@@ -374,8 +464,8 @@ struct Oracle {
             ry[i] = P.b_node[ibp][1] + P.b_edge[ibp][1] + t2;
             ++n_escapees;
           }
-          r0x[i] = rx[i] - ux[i] * dt;
-          r0y[i] = ry[i] - uy[i] * dt;
+          r0x[i] = rx[i] - val(ux[i]) * dt;
+          r0y[i] = ry[i] - val(uy[i]) * dt;
           u0x[i] = ux[i];
           u0y[i] = uy[i];
         }
@@ -424,33 +514,33 @@ struct Oracle {
     if (ncirc != 0) {
       for (int i = nbS; i < npfb; ++i) {
         for (int ib = 0; ib < ncirc; ++ib) {
-          double R = P.c_radius[ib];
-          double c_dir = R / std::fabs(R);
+          double Rc = P.c_radius[ib];
+          double c_dir = Rc / std::fabs(Rc);
           double ric1 = rx[i] - P.c_centre[ib][0], ric2 = ry[i] - P.c_centre[ib][1];
           double rad = std::sqrt(ric1 * ric1 + ric2 * ric2);
           if (c_dir > 0.0) {
-            if (rad <= R + sup_size) {
+            if (rad <= Rc + sup_size) {
               ric1 = ric1 / rad; ric2 = ric2 / rad;
               int k = push_mirror(i, 999 + ib + 1);
               if (k < 0) return error;
-              rx[k] = rx[i] - ric1 * 2.0 * (rad - R);
-              ry[k] = ry[i] - ric2 * 2.0 * (rad - R);
+              rx[k] = rx[i] - ric1 * 2.0 * (rad - Rc);
+              ry[k] = ry[i] - ric2 * 2.0 * (rad - Rc);
               double t1 = ric2, t2 = -ric1;
-              ux[k] = 2.0 * P.c_vel[ib][0] + 2.0 * t1 * R * P.c_omega[ib] - 1.0 * ux[i];
-              uy[k] = 2.0 * P.c_vel[ib][1] + 2.0 * t2 * R * P.c_omega[ib] - 1.0 * uy[i];
+              ux[k] = 2.0 * P.c_vel[ib][0] + 2.0 * t1 * Rc * P.c_omega[ib] - 1.0 * ux[i];
+              uy[k] = 2.0 * P.c_vel[ib][1] + 2.0 * t2 * Rc * P.c_omega[ib] - 1.0 * uy[i];
               theta[k] = 2.0 * P.c_thermal[ib] - 1.0 * theta[i];
               dP_mp[k] = dP(k, i);
             }
           } else if (c_dir < 0.0) {
-            if (rad >= std::fabs(R) - sup_size) {
+            if (rad >= std::fabs(Rc) - sup_size) {
               ric1 = ric1 / rad; ric2 = ric2 / rad;
               int k = push_mirror(i, 999 + ib + 1);
               if (k < 0) return error;
-              rx[k] = rx[i] + ric1 * 2.0 * (std::fabs(R) - rad);
-              ry[k] = ry[i] + ric2 * 2.0 * (std::fabs(R) - rad);
+              rx[k] = rx[i] + ric1 * 2.0 * (std::fabs(Rc) - rad);
+              ry[k] = ry[i] + ric2 * 2.0 * (std::fabs(Rc) - rad);
               double t1 = ric2, t2 = -ric1;
-              ux[k] = 2.0 * P.c_vel[ib][0] + 2.0 * t1 * std::fabs(R) * P.c_omega[ib] - 1.0 * ux[i];
-              uy[k] = 2.0 * P.c_vel[ib][1] + 2.0 * t2 * std::fabs(R) * P.c_omega[ib] - 1.0 * uy[i];
+              ux[k] = 2.0 * P.c_vel[ib][0] + 2.0 * t1 * std::fabs(Rc) * P.c_omega[ib] - 1.0 * ux[i];
+              uy[k] = 2.0 * P.c_vel[ib][1] + 2.0 * t2 * std::fabs(Rc) * P.c_omega[ib] - 1.0 * uy[i];
               theta[k] = 2.0 * P.c_thermal[ib] - 1.0 * theta[i];
               dP_mp[k] = dP(k, i);
             }
@@ -513,12 +603,12 @@ struct Oracle {
     // mirrors of moving solid particles copy their parent's velocity/temperature (:191-206)
     for (int j = npfb; j < npfb + nmirror; ++j) {
       int i = irelation[j];
-      double tmp = ux[i] * ux[i] + uy[i] * uy[i];
+      double tmp = val(ux[i] * ux[i] + uy[i] * uy[i]);
       if (i < nbS && tmp != 0.0) { ux[j] = ux[i]; uy[j] = uy[i]; }
     }
     for (int j = npfb; j < npfb + nmirror; ++j) {
       int i = irelation[j];
-      double tmp = theta[i] * theta[i];
+      double tmp = val(theta[i] * theta[i]);
       if (i < nbS && tmp != 0.0) theta[j] = theta[i];
     }
     // STEP 6: corners (:209-324)
@@ -655,7 +745,7 @@ struct Oracle {
     }
     for (int j = npfb; j < np; ++j) {
       int i = irelation[j];
-      double tmp = ux[i] * ux[i] + uy[i] * uy[i];
+      double tmp = val(ux[i] * ux[i] + uy[i] * uy[i]);
       if (i < nbS && tmp != 0.0) { ux[j] = ux[i]; uy[j] = uy[i]; }
     }
   }
@@ -666,10 +756,10 @@ struct Oracle {
       double nt1 = -n2, nt2 = n1;
       M2 Q{1.0 * n1 + 0.0 * n2, 1.0 * nt1 + 0.0 * nt2, 0.0 * n1 + 1.0 * n2, 0.0 * nt1 + 1.0 * nt2};
       M2 QT = tr(Q);
-      M2 T{tau[0][i], tau[2][i], tau[1][i], tau[3][i]};
-      M2 t = mm(QT, mm(T, Q));
+      M2T<R> T{tau[0][i], tau[2][i], tau[1][i], tau[3][i]};
+      M2T<R> t = mm(QT, mm(T, Q));
       t.a11 = -t.a11; t.a12 = -t.a12;
-      M2 o = mm(Q, mm(t, QT));
+      M2T<R> o = mm(Q, mm(t, QT));
       tau[0][j] = o.a11; tau[1][j] = o.a21; tau[2][j] = o.a12; tau[3][j] = o.a22;
     };
 #pragma omp parallel for schedule(static)
@@ -690,7 +780,7 @@ struct Oracle {
         } else if (P.b_type[ib] == 2 || P.b_type[ib] == 4) {
           for (int c = 0; c < 4; ++c) tau[c][j] = tau[c][i];
         } else if (P.b_type[ib] == 3) {
-          for (int c = 0; c < 4; ++c) tau[c][j] = 0.0;
+          for (int c = 0; c < 4; ++c) tau[c][j] = R(0.0);
         }
       }
       if (vr < 0 && vr > -npfb) {
@@ -917,12 +1007,13 @@ struct Oracle {
     }
     drx.assign(npfb, 0.0); dry.assign(npfb, 0.0);
     double maxU = 1.0e-10;
-    for (int i = 0; i < npfb; ++i) maxU = std::max(maxU, std::sqrt(ux[i] * ux[i] + uy[i] * uy[i]));
+    for (int i = 0; i < npfb; ++i)
+      maxU = std::max(maxU, std::sqrt(val(ux[i]) * val(ux[i]) + val(uy[i]) * val(uy[i])));
 #pragma omp parallel for schedule(static)
     for (int i = nbS; i < npfb; ++i) {
       double D;
       if (P.i_shift_coeff == 1) {
-        double absU = std::sqrt(ux[i] * ux[i] + uy[i] * uy[i]);
+        double absU = std::sqrt(val(ux[i]) * val(ux[i]) + val(uy[i]) * val(uy[i]));
         double temp = (double)0.2f * std::exp(-absU / ((double)0.2f * maxU));
         D = 4.0 * h * dt * (absU + temp * maxU);
       } else {
@@ -953,14 +1044,14 @@ struct Oracle {
   // ------------------------------------------------------------------ gradients
   // grad_operator (gradient_calculation.F90:50-147) for u, v, theta in one pass
   void grad_operators() {
-    for (auto& g : grad) g.assign(np, 0.0);
+    for (auto& g : grad) g.assign(np, R(0.0));
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < npfb; ++i) {
-      double a[6] = {0, 0, 0, 0, 0, 0};
+      R a[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
       for (int k = 0; k < ij_count[i]; ++k) {
         int j = L(k, i);
         double w1 = wGx[E(k, i)], w2 = wGy[E(k, i)];
-        double du = ux[j] - ux[i], dvv = uy[j] - uy[i], dth = theta[j] - theta[i];
+        R du = ux[j] - ux[i], dvv = uy[j] - uy[i], dth = theta[j] - theta[i];
         a[0] = a[0] + du * w1; a[1] = a[1] + du * w2;
         a[2] = a[2] + dvv * w1; a[3] = a[3] + dvv * w2;
         a[4] = a[4] + dth * w1; a[5] = a[5] + dth * w2;
@@ -977,13 +1068,13 @@ struct Oracle {
       int i = irelation[j];
       int vr = vrelation[j];
       for (int f = 0; f < 3; ++f) {
-        double g1 = grad[2 * f][i], g2 = grad[2 * f + 1][i];
-        double o1 = 0.0, o2 = 0.0;
+        R g1 = grad[2 * f][i], g2 = grad[2 * f + 1][i];
+        R o1 = 0.0, o2 = 0.0;
         bool set = false;
         auto reflect = [&](double r1, double r2, bool normal_zero) {
           double nn = std::sqrt(r1 * r1 + r2 * r2);
           double q11 = r1 / nn, q21 = r2 / nn, q12 = -q21, q22 = q11;
-          double b1 = q11 * g1 + q12 * g2, b2 = q21 * g1 + q22 * g2;
+          R b1 = q11 * g1 + q12 * g2, b2 = q21 * g1 + q22 * g2;
           if (normal_zero) b1 = 0.0; else b2 = -b2;
           o1 = q11 * b1 + q21 * b2;
           o2 = q12 * b1 + q22 * b2;
@@ -1021,63 +1112,77 @@ struct Oracle {
   }
 
   // ------------------------------------------------------------------ log-conformation
-  // calc_eigens (predictor_mod.F90:253-290)
-  static void calc_eigens(const M2& A, double& L1, double& L2, M2& R) {
-    double trc = A.a11 + A.a22;
-    double det = A.a11 * A.a22 - A.a21 * A.a12;
-    double tmp = 0.25 * trc * trc - det;
+  // calc_eigens (predictor_mod.F90:253-290), over the field type
+  template <class T>
+  static void calc_eigens(const M2T<T>& A, T& L1, T& L2, M2T<T>& Q) {
+    T trc = A.a11 + A.a22;
+    T det = A.a11 * A.a22 - A.a21 * A.a12;
+    T tmp = 0.25 * trc * trc - det;
     if (tmp <= 2.220446049250313e-16) tmp = 0.0;
-    L1 = 0.5 * trc + std::sqrt(tmp);
-    L2 = 0.5 * trc - std::sqrt(tmp);
+    L1 = 0.5 * trc + Sqrt(tmp);
+    L2 = 0.5 * trc - Sqrt(tmp);
     if (A.a21 != 0.0) {
-      double r11 = L1 - A.a22, r21 = A.a21;
-      double nrm = std::sqrt(r11 * r11 + r21 * r21);
+      T r11 = L1 - A.a22, r21 = A.a21;
+      T nrm = Sqrt(r11 * r11 + r21 * r21);
       r11 = r11 / nrm; r21 = r21 / nrm;
-      R = M2{r11, -r21, r21, r11};
+      Q = M2T<T>{r11, -r21, r21, r11};
     } else {
       L1 = A.a11; L2 = A.a22;
-      R = M2{1.0, 0.0, 0.0, 1.0};
+      Q = M2T<T>{1.0, 0.0, 0.0, 1.0};
+      diagonal_turn(A, Q);
     }
+  }
+  // The a21 == 0 branch returns Q = I, the limit of the general branch as a21 -> 0, where the
+  // eigenvector of L1 = a11 turns by a21 / (a11 - a22) (first order in a21, for a11 != a22).
+  // The derivative of the map A -> Q f(Lambda) Q^T keeps that turn; the branch's own constant
+  // Q would drop it.  The tangent carries it on Q's off-diagonal entries.
+  static void diagonal_turn(const M2T<double>&, M2T<double>&) {}
+  static void diagonal_turn(const M2T<Tan>& A, M2T<Tan>& Q) {
+    double gap = A.a11.v - A.a22.v;
+    if (gap == 0.0) return;
+    Q.a21.d = A.a21.d / gap;
+    Q.a12.d = -Q.a21.d;
   }
   // constitutive_eqn_evolve (predictor_mod.F90:141-251), Lagrangian, const_mod=2
   void constitutive_eqn_evolve() {
     const double eps_PTT = P.ve_nonlinearity;
     const double Wi = P.El * std::sqrt(P.Ra / P.Pr);
+    using MR = M2T<R>;
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < npfb; ++i) {
       // steps 1-2
-      M2 A{tau[0][i] / 1.0 + 1.0, tau[2][i] / 1.0 + 0.0, tau[1][i] / 1.0 + 0.0, tau[3][i] / 1.0 + 1.0};
-      A = M2{A.a11 / 1.0, A.a12 / 1.0, A.a21 / 1.0, A.a22 / 1.0};
-      double L1, L2; M2 R;
-      calc_eigens(A, L1, L2, R);
+      MR A{tau[0][i] / 1.0 + 1.0, tau[2][i] / 1.0 + 0.0, tau[1][i] / 1.0 + 0.0, tau[3][i] / 1.0 + 1.0};
+      A = MR{A.a11 / 1.0, A.a12 / 1.0, A.a21 / 1.0, A.a22 / 1.0};
+      R L1, L2; MR Q;
+      calc_eigens(A, L1, L2, Q);
       // step 3
-      M2 D{std::log(L1), 0.0, 0.0, std::log(L2)};
-      M2 Psi0 = mm(R, mm(D, tr(R)));
+      MR D{Log(L1), 0.0, 0.0, Log(L2)};
+      MR Psi0 = mm(Q, mm(D, tr(Q)));
       // step 5
-      M2 G{grad[0][i], grad[1][i], grad[2][i], grad[3][i]};  // G(a,b) = du_a/dx_b
-      M2 tm = mm(tr(R), mm(G, R));
-      double tmp1 = (L2 * tm.a12 + L1 * tm.a21) / (L2 - L1 + 1e-10);
+      MR G{grad[0][i], grad[1][i], grad[2][i], grad[3][i]};  // G(a,b) = du_a/dx_b
+      MR tm = mm(tr(Q), mm(G, Q));
+      R tmp1 = (L2 * tm.a12 + L1 * tm.a21) / (L2 - L1 + 1e-10);
       tm.a12 = 0.0; tm.a21 = 0.0;
-      M2 B = mm(R, mm(tm, tr(R)));
-      M2 W{0.0, tmp1, -tmp1, 0.0};
-      M2 Om = mm(R, mm(W, tr(R)));
+      MR B = mm(Q, mm(tm, tr(Q)));
+      MR W{0.0, tmp1, -tmp1, 0.0};
+      MR Om = mm(Q, mm(W, tr(Q)));
       // step 6
-      M2 OP = mm(Om, Psi0), PO = mm(Psi0, Om);
-      M2 t6{2.0 * B.a11 + OP.a11 - PO.a11, 2.0 * B.a12 + OP.a12 - PO.a12,
+      MR OP = mm(Om, Psi0), PO = mm(Psi0, Om);
+      MR t6{2.0 * B.a11 + OP.a11 - PO.a11, 2.0 * B.a12 + OP.a12 - PO.a12,
             2.0 * B.a21 + OP.a21 - PO.a21, 2.0 * B.a22 + OP.a22 - PO.a22};
       double dtl = dt;
-      M2 Psi{Psi0.a11 + dtl * t6.a11, Psi0.a12 + dtl * t6.a12, Psi0.a21 + dtl * t6.a21,
+      MR Psi{Psi0.a11 + dtl * t6.a11, Psi0.a12 + dtl * t6.a12, Psi0.a21 + dtl * t6.a21,
              Psi0.a22 + dtl * t6.a22};
       // step 7
-      calc_eigens(Psi, L1, L2, R);
-      L1 = std::exp(L1); L2 = std::exp(L2);
-      M2 E2{L1, 0.0, 0.0, L2};
-      A = mm(R, mm(E2, tr(R)));
+      calc_eigens(Psi, L1, L2, Q);
+      L1 = Exp(L1); L2 = Exp(L2);
+      MR E2{L1, 0.0, 0.0, L2};
+      A = mm(Q, mm(E2, tr(Q)));
       // step 8: f_relaxation_integrate (:318-331) with the old trace
-      double alpha_R = 1.0 + eps_PTT * (trace_conf[i] - 2.0);
-      double e1 = std::exp(-(alpha_R * 1.0 * dtl / Wi));
-      double e2 = (1.0 - e1) / 1.0;
-      A = M2{A.a11 * e1 + e2 * 1.0, A.a12 * e1 + e2 * 0.0, A.a21 * e1 + e2 * 0.0, A.a22 * e1 + e2 * 1.0};
+      R alpha_R = 1.0 + eps_PTT * (trace_conf[i] - 2.0);
+      R e1 = Exp(-(alpha_R * 1.0 * dtl / Wi));
+      R e2 = (1.0 - e1) / 1.0;
+      A = MR{A.a11 * e1 + e2 * 1.0, A.a12 * e1 + e2 * 0.0, A.a21 * e1 + e2 * 0.0, A.a22 * e1 + e2 * 1.0};
       // step 9
       trace_conf[i] = A.a11 + A.a22;
       tau[0][i] = 1.0 * (1.0 * A.a11 - 1.0);
@@ -1097,49 +1202,49 @@ struct Oracle {
     const double cs = P.beta * std::sqrt(P.Pr / P.Ra);
     const double cp = (1.0 - P.beta) * P.Pr / (P.Ra * P.El);
     const double ct = 1.0 / std::sqrt(P.Ra * P.Pr);
-    std::vector<double> rh1(npfb), rh2(npfb), rht(npfb);
+    std::vector<R> rh1(npfb), rh2(npfb), rht(npfb);
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < npfb; ++i) {
-      double s1 = 0, s2 = 0, st = 0;
+      R s1 = 0.0, s2 = 0.0, st = 0.0;
       M2 Kc = K(i);
       for (int k = 0; k < ij_count[i]; ++k) {
         int j = L(k, i);
-        double u1 = ux[i] - ux[j], u2 = uy[i] - uy[j];
+        R u1 = ux[i] - ux[j], u2 = uy[i] - uy[j];
         double w1 = wGx[E(k, i)], w2 = wGy[E(k, i)], wl = wL[E(k, i)];
         if (P.const_mod == 1) {
           s1 = s1 + cs * u1 * wl;
           s2 = s2 + cs * u2 * wl;
         } else {
-          double T11 = tau[0][j] - tau[0][i], T21 = tau[1][j] - tau[1][i];
-          double T12 = tau[2][j] - tau[2][i], T22 = tau[3][j] - tau[3][i];
+          R T11 = tau[0][j] - tau[0][i], T21 = tau[1][j] - tau[1][i];
+          R T12 = tau[2][j] - tau[2][i], T22 = tau[3][j] - tau[3][i];
           double kw1 = Kc.a11 * w1 + Kc.a12 * w2, kw2 = Kc.a21 * w1 + Kc.a22 * w2;
-          double tw1 = T11 * kw1 + T12 * kw2, tw2 = T21 * kw1 + T22 * kw2;
+          R tw1 = T11 * kw1 + T12 * kw2, tw2 = T21 * kw1 + T22 * kw2;
           s1 = s1 + cp * tw1 + cs * u1 * wl;
           s2 = s2 + cp * tw2 + cs * u2 * wl;
         }
-        double thij = theta[i] - theta[j];
+        R thij = theta[i] - theta[j];
         st = st + ct * thij * wl;
       }
       rh1[i] = s1; rh2[i] = s2; rht[i] = st;
     }
     // the circle mirrors' share of the same sums (the drag diagnostic; no reference counterpart)
-    circ_s1.assign(npfb, 0.0); circ_s2.assign(npfb, 0.0);
+    circ_s1.assign(npfb, R(0.0)); circ_s2.assign(npfb, R(0.0));
     if (P.nb_circles > 0) {
 #pragma omp parallel for schedule(static)
       for (int i = nbS; i < npfb; ++i) {
-        double s1 = 0, s2 = 0;
+        R s1 = 0.0, s2 = 0.0;
         M2 Kc = K(i);
         for (int k = 0; k < ij_count[i]; ++k) {
           int j = L(k, i);
           if (j < npfb || vrelation[j] <= 999) continue;
-          double u1 = ux[i] - ux[j], u2 = uy[i] - uy[j];
+          R u1 = ux[i] - ux[j], u2 = uy[i] - uy[j];
           double w1 = wGx[E(k, i)], w2 = wGy[E(k, i)], wl = wL[E(k, i)];
           if (P.const_mod == 1) {
             s1 = s1 + cs * u1 * wl;
             s2 = s2 + cs * u2 * wl;
           } else {
-            double T11 = tau[0][j] - tau[0][i], T21 = tau[1][j] - tau[1][i];
-            double T12 = tau[2][j] - tau[2][i], T22 = tau[3][j] - tau[3][i];
+            R T11 = tau[0][j] - tau[0][i], T21 = tau[1][j] - tau[1][i];
+            R T12 = tau[2][j] - tau[2][i], T22 = tau[3][j] - tau[3][i];
             double kw1 = Kc.a11 * w1 + Kc.a12 * w2, kw2 = Kc.a21 * w1 + Kc.a22 * w2;
             s1 = s1 + cp * (T11 * kw1 + T12 * kw2) + cs * u1 * wl;
             s2 = s2 + cp * (T21 * kw1 + T22 * kw2) + cs * u2 * wl;
@@ -1242,17 +1347,48 @@ struct Oracle {
     LS_iters = iter;
   }
 
+  // The PPE solve over the field type.  With R = Tan the system is solved twice on the same
+  // matrix: the values (the step's own solve, which sets LS_iters and LS_residual) and then the
+  // derivatives, A dP = dB, from a zero start.  dB is scaled to unit RMS for that solve and the
+  // result scaled back, since the solver's rule that a first residual norm <= 1e-6 makes the
+  // tolerance absolute would otherwise stop a small tangent after one iteration.
+  int tangent_iters = 0;
+  void solve_system(std::vector<R>& x, const std::vector<R>& B) {
+    const bool nonull = P.i_open_domain == 0;
+    if constexpr (std::is_same<R, double>::value) {
+      bicgstab(x, B, nonull);
+    } else {
+      std::vector<double> xv(npfb), bv(npfb), xd(npfb, 0.0), bd(npfb);
+      for (int i = 0; i < npfb; ++i) { xv[i] = x[i].v; bv[i] = B[i].v; bd[i] = B[i].d; }
+      bicgstab(xv, bv, nonull);
+      const int it = LS_iters;
+      const double res = LS_residual;
+      const int warn = warnings;
+      double ms = chunk_sum(0, npfb, [&](int64_t i) { return bd[i] * bd[i]; }) / (double)npfb;
+      tangent_iters = 0;
+      if (ms > 0.0) {
+        const double rms = std::sqrt(ms);
+        for (auto& v : bd) v = v / rms;
+        bicgstab(xd, bd, nonull);
+        tangent_iters = LS_iters;
+        for (auto& v : xd) v = v * rms;
+      }
+      LS_iters = it; LS_residual = res; warnings = warn;
+      for (int i = 0; i < npfb; ++i) x[i] = Tan(xv[i], xd[i]);
+    }
+  }
+
   // ppe_solve_in_house_simple_dirichlet (ppe_solve_in_house_simple_dirichlet.F90:1-158)
   void ppe_solve() {
-    ppe_B.assign(npfb, 0.0);
+    ppe_B.assign(npfb, R(0.0));
     const double dtl = dt;
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < npfb; ++i) {
-      double fb = 0.0;
+      R fb = 0.0;
       M2 Kc = K(i);
       for (int k = 0; k < ij_count[i]; ++k) {
         int j = L(k, i);
-        double u1 = ux[i] - ux[j], u2 = uy[i] - uy[j];
+        R u1 = ux[i] - ux[j], u2 = uy[i] - uy[j];
         double w1 = wGx[E(k, i)], w2 = wGy[E(k, i)];
         double kw1 = Kc.a11 * w1 + Kc.a12 * w2, kw2 = Kc.a21 * w1 + Kc.a22 * w2;
         fb = fb - (u1 * kw1 + u2 * kw2);
@@ -1261,9 +1397,9 @@ struct Oracle {
     }
     ppe_rhs_mean = 0.0;
     if (P.i_open_domain == 0) {
-      double temp = chunk_sum(0, npfb, [&](int64_t i) { return ppe_B[i]; });
+      R temp = chunk_sum(0, npfb, [&](int64_t i) { return ppe_B[i]; });
       temp = temp / (double)npfb;
-      ppe_rhs_mean = temp;
+      ppe_rhs_mean = val(temp);
       for (int i = 0; i < npfb; ++i) ppe_B[i] = ppe_B[i] - temp;
     }
     // assembly: one ELL slot per neighbour; duplicate parent columns accumulate into the
@@ -1318,12 +1454,12 @@ struct Oracle {
         for (int k = 0; k < ij_count[i]; ++k) ppe_val[E(k, i)] = ppe_val[E(k, i)] * ppe_smooth[i];
       }
     }
-    std::vector<double> x(npfb, 0.0);
+    std::vector<R> x(npfb, R(0.0));
     if (P.ppe_warm_start)  // opt-in: start from the previous step's P (the reference uses 0)
       for (int i = 0; i < npfb; ++i) x[i] = p[i];
     mark(10);
     double t0 = wtime();
-    bicgstab(x, ppe_B, P.i_open_domain == 0);
+    solve_system(x, ppe_B);
     t_solve_ms = (wtime() - t0) * 1e3;
     mark(9);
     for (int i = 0; i < npfb; ++i) p[i] = x[i];
@@ -1332,13 +1468,13 @@ struct Oracle {
   // calc_pressure_gradient (gradient_calculation.F90:16-48)
   void calc_pressure_gradient() {
     for (int j = npfb; j < np; ++j) p[j] = p[irelation[j]] + dP_mp[j];
-    gpx.assign(npfb, 0.0); gpy.assign(npfb, 0.0);
+    gpx.assign(npfb, R(0.0)); gpy.assign(npfb, R(0.0));
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < npfb; ++i) {
-      double a = 0, b = 0;
+      R a = 0.0, b = 0.0;
       for (int k = 0; k < ij_count[i]; ++k) {
         int j = L(k, i);
-        double temp = p[j] - p[i];
+        R temp = p[j] - p[i];
         a = a + temp * wGx[E(k, i)];
         b = b + temp * wGy[E(k, i)];
       }
@@ -1350,15 +1486,15 @@ struct Oracle {
     // pressure gradient - circle-mirror share of the viscous/polymeric sums)
     circle_fx = circle_fy = 0.0;
     if (P.nb_circles > 0) {
-      std::vector<double> fx(npfb, 0.0), fy(npfb, 0.0);
+      std::vector<R> fx(npfb, R(0.0)), fy(npfb, R(0.0));
 #pragma omp parallel for schedule(static)
       for (int i = nbS; i < npfb; ++i) {
         if (inbin[i]) continue;
-        double a = 0, b = 0;
+        R a = 0.0, b = 0.0;
         for (int k = 0; k < ij_count[i]; ++k) {
           int j = L(k, i);
           if (j < npfb || vrelation[j] <= 999) continue;
-          double temp = p[j] - p[i];
+          R temp = p[j] - p[i];
           a = a + temp * wGx[E(k, i)];
           b = b + temp * wGy[E(k, i)];
         }
@@ -1366,8 +1502,8 @@ struct Oracle {
         fx[i] = P.dv * ((Kc.a11 * a + Kc.a12 * b) - circ_s1[i]);
         fy[i] = P.dv * ((Kc.a21 * a + Kc.a22 * b) - circ_s2[i]);
       }
-      circle_fx = chunk_sum(0, npfb, [&](int64_t i) { return fx[i]; });
-      circle_fy = chunk_sum(0, npfb, [&](int64_t i) { return fy[i]; });
+      circle_fx = val(chunk_sum(0, npfb, [&](int64_t i) { return fx[i]; }));
+      circle_fy = val(chunk_sum(0, npfb, [&](int64_t i) { return fy[i]; }));
     }
   }
 
@@ -1395,8 +1531,8 @@ struct Oracle {
       double n1 = rx[i] - rx[j], n2 = ry[i] - ry[j];
       double t = std::sqrt(n1 * n1 + n2 * n2);
       n1 = n1 / t; n2 = n2 / t;
-      double u1 = ux[i] - ux[j], u2 = uy[i] - uy[j];
-      double un = u1 * n1 + u2 * n2;
+      R u1 = ux[i] - ux[j], u2 = uy[i] - uy[j];
+      R un = u1 * n1 + u2 * n2;
       if (un <= 0.0) { ux[i] = ux[i] - un * n1; uy[i] = uy[i] - un * n2; }
     }
   }
@@ -1405,15 +1541,15 @@ struct Oracle {
   void secondary_properties() {
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < npfb; ++i) {
-      double vt = 0.0;
+      R vt = 0.0;
       for (int k = 0; k < ij_count[i]; ++k) {
         int j = L(k, i);
-        double tmp = (uy[i] - uy[j]) * wGx[E(k, i)] - (ux[i] - ux[j]) * wGy[E(k, i)];
+        R tmp = (uy[i] - uy[j]) * wGx[E(k, i)] - (ux[i] - ux[j]) * wGy[E(k, i)];
         vt = vt - tmp;
       }
       vort[i] = vt;
     }
-    double s = chunk_sum(0, npfb, [&](int64_t i) { return ux[i] * ux[i] + uy[i] * uy[i]; });
+    double s = val(chunk_sum(0, npfb, [&](int64_t i) { return ux[i] * ux[i] + uy[i] * uy[i]; }));
     rms_u = std::sqrt(s / (double)npfb);
   }
 
@@ -1445,15 +1581,30 @@ struct Oracle {
     error = 0; warnings = 0; n_escapees = 0;
     // STEP 1 (div_free.F90:39-41)
     r0x.assign(2 * npfb, 0.0); r0y.assign(2 * npfb, 0.0);
-    u0x.assign(2 * npfb, 0.0); u0y.assign(2 * npfb, 0.0);
+    u0x.assign(2 * npfb, R(0.0)); u0y.assign(2 * npfb, R(0.0));
     for (int i = 0; i < npfb; ++i) { u0x[i] = ux[i]; u0y[i] = uy[i]; r0x[i] = rx[i]; r0y[i] = ry[i]; }
     // STEP 2
     set_time_step();
+    const bool replay = geo_mode == 2 && geo_step < geo_dt.size();
+    if (replay) dt = geo_dt[geo_step];
     // STEP 3
-    for (int i = nbS; i < npfb; ++i) { rx[i] = r0x[i] + u0x[i] * dt; ry[i] = r0y[i] + u0y[i] * dt; }
+    for (int i = nbS; i < npfb; ++i) {
+      rx[i] = r0x[i] + val(u0x[i]) * dt;
+      ry[i] = r0y[i] + val(u0y[i]) * dt;
+    }
+    if (replay) {
+      std::copy(geo_rx[geo_step].begin(), geo_rx[geo_step].end(), rx.begin());
+      std::copy(geo_ry[geo_step].begin(), geo_ry[geo_step].end(), ry.begin());
+    }
     // STEP 4
     int st = put_in_bin(xmn, xmx, ymn, ymx);
     if (st) return st;
+    if (geo_mode == 1) {
+      geo_rx.emplace_back(rx.begin(), rx.begin() + npfb);
+      geo_ry.emplace_back(ry.begin(), ry.begin() + npfb);
+      geo_dt.push_back(dt);
+    }
+    if (geo_mode != 0) ++geo_step;
     mark(1);
     st = create_mirror_particles();
     if (st) return st;
@@ -1473,7 +1624,7 @@ struct Oracle {
     ushx.assign(npfb, 0.0); ushy.assign(npfb, 0.0);
     new_fick_shift();
     for (int i = 0; i < npfb; ++i) { ushx[i] = drx[i] / dt; ushy[i] = dry[i] / dt; }
-    for (int i = 0; i < nbS; ++i) { ushx[i] = -ux[i]; ushy[i] = -uy[i]; }
+    for (int i = 0; i < nbS; ++i) { ushx[i] = -val(ux[i]); ushy[i] = -val(uy[i]); }
     // STEP 7
     mark(8);
     prediction_step();
@@ -1502,8 +1653,8 @@ struct Oracle {
     mark(12);
     // STEP 12
     for (int i = nbS; i < npfb; ++i) {
-      rx[i] = r0x[i] + 0.5 * (ux[i] + u0x[i]) * dt + ushx[i] * dt;
-      ry[i] = r0y[i] + 0.5 * (uy[i] + u0y[i]) * dt + ushy[i] * dt;
+      rx[i] = r0x[i] + val(0.5 * (ux[i] + u0x[i])) * dt + ushx[i] * dt;
+      ry[i] = r0y[i] + val(0.5 * (uy[i] + u0y[i])) * dt + ushy[i] * dt;
     }
     time += dt;
     return VEBI_OK;
@@ -1514,8 +1665,8 @@ struct Oracle {
     s->dt = dt; s->LS_residual = LS_residual; s->umax = umax;
     double mu = 0, mv = 0, mp = 0;
     for (int i = 0; i < npfb; ++i) {
-      mu = std::max(mu, std::fabs(ux[i])); mv = std::max(mv, std::fabs(uy[i]));
-      mp = std::max(mp, std::fabs(p[i]));
+      mu = std::max(mu, std::fabs(val(ux[i]))); mv = std::max(mv, std::fabs(val(uy[i])));
+      mp = std::max(mp, std::fabs(val(p[i])));
     }
     s->max_abs_u = mu; s->max_abs_v = mv; s->max_abs_p = mp;
     s->rms_u = rms_u; s->ppe_rhs_mean = ppe_rhs_mean;
@@ -1531,8 +1682,10 @@ struct Oracle {
 
   // ------------------------------------------------------------------ inspection
   struct View { const void* p; int64_t esz, n; };
+  static View view_of(const std::vector<double>& v, int64_t n) { return View{v.data(), 8, n}; }
+  static View view_of(const std::vector<Tan>&, int64_t) { return View{nullptr, 0, -1}; }
   View view(const std::string& nm) const {
-    auto D = [](const std::vector<double>& v, int64_t n) { return View{v.data(), 8, n}; };
+    auto D = [](const auto& v, int64_t n) { return view_of(v, n); };
     auto I = [](const std::vector<int>& v, int64_t n) { return View{v.data(), 4, n}; };
     int64_t ell = (int64_t)std::max(maxneighbours, 1) * npfb;
     if (nm == "rx") return D(rx, np);
@@ -1589,9 +1742,26 @@ struct Oracle {
     if (nm == "div_r") return D(div_r, npfb);
     return View{nullptr, 0, -1};
   }
+  // the fields of the tangent-linear model, by name, with their lengths
+  const std::vector<R>* field(const std::string& nm, int64_t* n) const {
+    *n = np;
+    if (nm == "ux") return &ux;
+    if (nm == "uy") return &uy;
+    if (nm == "theta") return &theta;
+    if (nm == "p") return &p;
+    if (nm == "tau11") return &tau[0];
+    if (nm == "tau21") return &tau[1];
+    if (nm == "tau12") return &tau[2];
+    if (nm == "tau22") return &tau[3];
+    *n = npfb;
+    if (nm == "trace_conf") return &trace_conf;
+    if (nm == "ppe_B") return &ppe_B;
+    return nullptr;
+  }
 };
 
-thread_local std::string g_err;
+using Oracle = OracleT<double>;
+using OracleTan = OracleT<Tan>;
 
 }  // namespace
 
@@ -1616,6 +1786,64 @@ int orc_step(void* h, double xmn, double ymn, double xmx, double ymx, int second
   if (st) { o->fill_stats(st); st->error = s; }
   return s;
 }
+// geometry record/replay of an FP64 oracle: 1 starts a record (clearing the last), 2 replays
+// the record from its first step, 0 turns both off and drops the record
+int orc_geometry(void* h, int mode) {
+  auto* o = static_cast<Oracle*>(h);
+  if (mode < 0 || mode > 2) return VEBI_ERR_ARG;
+  if (mode != 2) { o->geo_rx.clear(); o->geo_ry.clear(); o->geo_dt.clear(); }
+  o->geo_mode = mode;
+  o->geo_step = 0;
+  return 0;
+}
+
+// ---- FP64 tangent-linear model of the step (the oracle over forward-mode dual numbers)
+void* orc_tlm_create(const vebi_params* p, int* status) {
+  auto* o = new OracleTan();
+  int st = o->create(p);
+  if (status) *status = st;
+  if (st) { delete o; return nullptr; }
+  return o;
+}
+int orc_tlm_destroy(void* h) { delete static_cast<OracleTan*>(h); return 0; }
+int orc_tlm_set_state(void* h, const double* r, const double* u, const double* tp, const double* th,
+                      const double* tc, const uint8_t* ib, int ld) {
+  return static_cast<OracleTan*>(h)->set_state(r, u, tp, th, tc, ib, ld);
+}
+int orc_tlm_set_tangent(void* h, const double* du, const double* dtp, const double* dth, int ld) {
+  return static_cast<OracleTan*>(h)->set_tangent(du, dtp, dth, ld);
+}
+int orc_tlm_step(void* h, double xmn, double ymn, double xmx, double ymx, vebi_step_stats* st,
+                 int* tangent_iters) {
+  auto* o = static_cast<OracleTan*>(h);
+  int s = o->step(xmn, ymn, xmx, ymx, 0);
+  if (st) { o->fill_stats(st); st->error = s; }
+  if (tangent_iters) *tangent_iters = o->tangent_iters;
+  return s;
+}
+int orc_tlm_size(void* h, const char* name, int64_t* n) {
+  return static_cast<OracleTan*>(h)->field(name, n) ? 0 : VEBI_ERR_ARG;
+}
+int orc_tlm_get(void* h, const char* name, double* value, double* tangent, int64_t n) {
+  int64_t m = 0;
+  const auto* f = static_cast<OracleTan*>(h)->field(name, &m);
+  if (!f || n < m) return VEBI_ERR_ARG;
+  for (int64_t i = 0; i < m; ++i) {
+    if (value) value[i] = (*f)[i].v;
+    if (tangent) tangent[i] = (*f)[i].d;
+  }
+  return 0;
+}
+int orc_tlm_box(void* h, double* box4) {
+  auto* o = static_cast<OracleTan*>(h);
+  box4[0] = o->x_mint; box4[1] = o->x_maxt; box4[2] = o->y_mint; box4[3] = o->y_maxt;
+  return 0;
+}
+int orc_tlm_set_itermax(void* h, int itermax) {
+  static_cast<OracleTan*>(h)->P.itermax = itermax;
+  return 0;
+}
+
 int orc_set_itermax(void* h, int itermax) {
   static_cast<Oracle*>(h)->P.itermax = itermax;
   return 0;
@@ -1641,9 +1869,9 @@ int orc_get(void* h, const char* name, void* out, int64_t bytes) {
 double orc_kernel_w(void* h, double q) { return static_cast<Oracle*>(h)->Wab(q); }
 double orc_kernel_fac(void* h, double q) { return static_cast<Oracle*>(h)->fac(q); }
 int orc_eigens(const double* A4, double* L2, double* R4) {
-  M2 A{A4[0], A4[1], A4[2], A4[3]}, R;
-  Oracle::calc_eigens(A, L2[0], L2[1], R);
-  R4[0] = R.a11; R4[1] = R.a12; R4[2] = R.a21; R4[3] = R.a22;
+  M2 A{A4[0], A4[1], A4[2], A4[3]}, Q;
+  Oracle::calc_eigens(A, L2[0], L2[1], Q);
+  R4[0] = Q.a11; R4[1] = Q.a12; R4[2] = Q.a21; R4[3] = Q.a22;
   return 0;
 }
 int orc_threads(void) {
