@@ -1,6 +1,12 @@
-"""Reverse mode of the step (vebi_adjoint_*) against central finite differences of the same
-differentiated map (the steps replayed with the recorded geometry), on a small heated cavity
-(Oldroyd-B, Ra=1e4) after a spin-up, over a window of 6 steps with checkpoints every 4.
+"""Reverse mode of the step (vebi_adjoint_*) against two references of the same differentiated
+map (the steps replayed with the recorded geometry), on a small heated cavity (Oldroyd-B,
+Ra=1e4) after a spin-up, over a window of 6 steps with checkpoints every 4:
+
+* central finite differences of the GPU's own replayed window;
+* the oracle's FP64 tangent-linear model (oracle.TangentLinear: the CPU restatement of the step
+  run over forward-mode dual numbers, with the geometry of the unperturbed trajectory), started
+  from the state the GPU reached.  It needs no step size, so it also checks the stress path of
+  the Oldroyd-B channel, where the log-conformation update's pole defeats finite differences.
 
 J = mean kinetic energy of the fluid particles after the window.  The PPE runs to a relative
 residual of 1e-12 so that its truncation stays far below the differences (step 1e-3 on unit-max
@@ -8,6 +14,7 @@ directions: truncation and solver noise are both ~1e-7 relative here)."""
 import numpy as np
 import pytest
 
+from oracle.oracle import TangentLinear
 from vebisph_gb300 import abi, cases
 from vebisph_gb300.solver import Adjoint, StepSolver
 
@@ -63,6 +70,38 @@ def central(w, field, direction):
     return (jp - jm) / (2.0 * EPS)
 
 
+def direction(w, field, seed):
+    """A seeded direction over the fluid particles, scaled to the field's largest entry."""
+    case, st0 = w["case"], w["st0"]
+    rng = np.random.default_rng(seed)
+    shape = st0[field].shape
+    d = np.zeros(shape)
+    d[..., case.nbS:] = rng.normal(size=shape[:-1] + (case.npfb - case.nbS,))
+    if field == "tau":
+        d[2] = d[1]  # a symmetric perturbation, as the conformation is
+    return d * (max(np.abs(st0[field]).max(), 1.0e-3) / np.abs(d).max())
+
+
+def tangent_linear(w, field, d):
+    """dJ . d from the oracle's FP64 tangent-linear model of the window, from the GPU's state."""
+    case, n, nbS = w["case"], w["case"].npfb, w["case"].nbS
+    t = TangentLinear(case, state=w["st0"])
+    t.set_direction(**{{"u": "du", "tau": "dtau", "theta": "dtheta"}[field]: d})
+    for _ in range(NSTEPS):
+        t.step()
+    (ux, dux), (uy, duy) = t.get("ux"), t.get("uy")
+    t.close()
+    return float(np.sum(ux[nbS:n] * dux[nbS:n] + uy[nbS:n] * duy[nbS:n]) / (n - nbS))
+
+
+def check_tangent_linear(w, field, seed, rtol):
+    d = direction(w, field, seed)
+    tl = tangent_linear(w, field, d)
+    ad = float(np.sum(w["g"][field] * d))
+    assert abs(tl) > 0
+    assert abs(ad - tl) <= rtol * abs(tl), (ad, tl)
+
+
 def test_replay_reproduces_the_record(window):
     assert run_from(window) == window["J0"]
 
@@ -109,6 +148,12 @@ def test_stress_gradient_matches_central_differences(window, k):
     fd = central(window, "tau", d)
     ad = float(np.sum(window["g"]["tau"] * d))
     assert abs(fd - ad) <= RTOL * abs(fd), (fd, ad)
+
+
+@pytest.mark.parametrize("field", ["theta", "u", "tau"])
+def test_gradient_matches_the_tangent_linear_model(window, field):
+    """Measured on GB300: within 8e-12 for every field, with either solver."""
+    check_tangent_linear(window, field, 10, 1.0e-9)
 
 
 def test_weissenberg_gradient_matches_central_differences(window):
@@ -186,6 +231,39 @@ def test_channel_gradient_matches_central_differences(channel, field):
     assert abs(fd - ad) <= RTOL * abs(fd), (fd, ad)
 
 
+@pytest.fixture(scope="module")
+def oldroyd_b_channel():
+    """Oldroyd-B Poiseuille (Wi=1, beta=0.1): conformations near the update's pole, where central
+    differences stay ~1e-4 off whatever the step; the tangent-linear model has no step.
+
+    Near the pole the map also amplifies rounding: over the window the GPU's and the oracle's
+    trajectories from the same state part by 5e-10 in u (5e-12 or less in the other windows), and
+    the derivative, evaluated along each, moves with them.  Measured on GB300: the velocity
+    gradient agrees within 2e-6; the stress gradient, whose direction acts on the conformations
+    directly, within ~1e-4, which checks nothing and is not tested."""
+    case = cases.poiseuille(24, seed=5)
+    case.tol = 1.0e-12
+    case.itermax = 4000
+    s = StepSolver(case)
+    for _ in range(SPIN):
+        s.step()
+    st0 = s.download()
+    adj = Adjoint(s, max_steps=NSTEPS, checkpoint_every=K)
+    adj.record(NSTEPS)
+    fin = s.download()
+    nbS, n = case.nbS, case.npfb
+    seed = np.zeros((2, n))
+    seed[:, nbS:] = fin["u"][:, nbS:] / (n - nbS)
+    g = adj.reverse(seed_u=seed)
+    yield dict(case=case, s=s, adj=adj, st0=st0, g=g)
+    adj.close()
+    s.close()
+
+
+def test_oldroyd_b_channel_gradient_matches_the_tangent_linear_model(oldroyd_b_channel):
+    check_tangent_linear(oldroyd_b_channel, "u", 10, 1.0e-5)
+
+
 @pytest.fixture(scope="module", params=[1, 2])
 def cylinder_window(request):
     """Confined cylinder (circle mirrors, walls, periodic patches), Newtonian and Oldroyd-B,
@@ -224,3 +302,8 @@ def test_cylinder_velocity_gradient_matches_central_differences(cylinder_window)
     ad = float(np.sum(w["g"]["u"] * d))
     assert abs(fd) > 0
     assert abs(fd - ad) <= RTOL * abs(fd), (fd, ad)
+
+
+def test_cylinder_gradient_matches_the_tangent_linear_model(cylinder_window):
+    """Measured on GB300: within 5e-11 (Newtonian) and 4e-10 (Oldroyd-B)."""
+    check_tangent_linear(cylinder_window, "u", 10, 1.0e-8)
