@@ -361,7 +361,8 @@ def run_gb300(args, dist: Dist):
 def run_adjoint(args, dist: Dist) -> dict:
     """Reverse mode on the heated-cavity workload (differentially heated square cavity,
     args.adjoint_side^2 fluid particles, Ra=1e5, Pr=1, Oldroyd-B Wi=0.5, beta=0.5, seeded
-    perturbed temperature), FP64 step with the reference's PPE solver: J = mean kinetic energy
+    perturbed temperature), FP64 or mixed-precision step (args.adjoint_precision) with the
+    reference's PPE solver or the multigrid (args.precond): J = mean kinetic energy
     after a window of args.adjoint steps, dJ/dtheta0 (full field) and dJ/dWi, checkpoints every
     args.checkpoint steps.  Forward cost = the plain steps of the window (captured graph);
     adjoint cost = the reverse sweep, its recompute of every segment included.  With
@@ -377,7 +378,8 @@ def run_adjoint(args, dist: Dist) -> dict:
     case.tol = args.adjoint_tol
     if args.precond == "multigrid":
         case.ppe_precond = abi.PRECOND_MULTIGRID
-    s = StepSolver(case)
+    mixed = args.adjoint_precision == "mixed"
+    s = StepSolver(case, precision=abi.PREC_MIXED if mixed else abi.PREC_FP64)
     for _ in range(max(args.warmup, args.adjoint_spinup)):
         s.step()
     st0 = s.download()
@@ -419,9 +421,12 @@ def run_adjoint(args, dist: Dist) -> dict:
     solver = ("the multigrid-preconditioned PPE (forward and transposed)" if args.precond == "multigrid"
               else "the reference's PPE solver")
     model = "Oldroyd-B Wi=0.5 beta=0.5" if case.const_mod != 1 else "Newtonian (const_mod 1) beta=0.5"
+    step = ("mixed-precision step (FP32 pair sums and SpMV; the VJP in FP64 on its widened weights, "
+            "the transposed solve in FP64)" if mixed else "FP64 step")
     return {"workload": f"{case.name}: heated cavity, {n - nbS} fluid + {nbS} wall particles, Ra=1e5 Pr=1 "
-                        f"{model}, FP64 step, {solver}, PPE tol {case.tol:g}, {args.adjoint_spinup} steps "
+                        f"{model}, {step}, {solver}, PPE tol {case.tol:g}, {args.adjoint_spinup} steps "
                         f"of spin-up",
+            "precision": args.adjoint_precision,
             "window_steps": N, "checkpoint_every": K, "J": J,
             "forward_ms_per_step": 1e3 * t_fwd / N, "record_ms_per_step": 1e3 * t_rec / N,
             "reverse_ms_per_step": 1e3 * t_rev / N, "adjoint_over_forward": t_rev / t_fwd,
@@ -707,6 +712,8 @@ def main():
     ap.add_argument("--adjoint-tol", type=float, default=1.0e-8, help="PPE tolerance of the adjoint workload")
     ap.add_argument("--adjoint-spinup", type=int, default=20, help="steps run before the adjoint window")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement of the default line")
+    ap.add_argument("--adjoint-precision", default="fp64", choices=["fp64", "mixed"],
+                    help="arithmetic of the adjoint workload's forward step")
     ap.add_argument("--adjoint-const-mod", type=int, default=2, choices=[1, 2],
                     help="constitutive model of the adjoint workload: 2 Oldroyd-B, 1 Newtonian")
     args = ap.parse_args()
@@ -757,7 +764,11 @@ def main():
             aargs = argparse.Namespace(**vars(args))
             aargs.adjoint, aargs.checkpoint, aargs.precond = 20, 5, "multigrid"
             aargs.adjoint_tol, aargs.adjoint_fd, aargs.adjoint_const_mod = 1.0e-8, 0, 2
+            aargs.adjoint_precision = "fp64"
             res["adjoint"] = run_adjoint(aargs, dist)
+            # the same window with the mixed-precision forward step (the configuration's FP32 step)
+            aargs.adjoint_precision = "mixed"
+            res["adjoint_mixed"] = run_adjoint(aargs, dist)
         res.pop("_fields", None)
     else:
         from oracle import build as ob

@@ -289,8 +289,10 @@ const char* vebi_last_error(void);
  * the context's fields at an intermediate state.
  *
  * Scope: closed domains with wall and periodic patches (and their corners) and circles,
- * Newtonian or Oldroyd-B (ve_nonlinearity = 0), FP64 contexts, no PPE warm start, no
- * correct_velocity; other contexts get VEBI_ERR_ARG from vebi_adjoint_create.  Destroy the
+ * Newtonian or Oldroyd-B (ve_nonlinearity = 0), FP64 or mixed-precision contexts, no PPE warm
+ * start, no correct_velocity; other contexts get VEBI_ERR_ARG from vebi_adjoint_create.  In a
+ * mixed-precision context the window runs the mixed step and the VJP, in FP64, uses the FP32
+ * weights that step used; its transposed solve is the context's mixed solver.  Destroy the
  * adjoint before its context. */
 typedef struct vebi_adjoint vebi_adjoint;
 /* Set the Weissenberg number of a context (El = Wi sqrt(Pr/Ra), Ra, Pr, beta unchanged): the

@@ -29,8 +29,12 @@
 // parents, so the reverse sweep is deterministic.
 //
 // Supported: closed domains with wall (b_type 1) and periodic (b_type 2) patches and their
-// corners, circles, Newtonian or Oldroyd-B (ve_nonlinearity = 0), FP64 arithmetic.  The
-// adjoint also returns dJ/dWi (El = Wi sqrt(Pr/Ra) with Ra, Pr, beta fixed): Wi enters the
+// corners, circles, Newtonian or Oldroyd-B (ve_nonlinearity = 0), FP64 or mixed-precision
+// contexts.  In a mixed context the window runs the mixed step (FP32 weights and correction
+// matrices, FP32 pair sums); the tape widens the step's FP32 weights and correction matrices to
+// FP64, so the VJP, in FP64, is that of the mixed map with the weights it used, exact up to the
+// FP32 rounding of its pair sums; the transposed solve runs the context's mixed solver (FP64
+// recurrences, FP32 SpMV) on an FP32 copy of A^T.  The adjoint also returns dJ/dWi (El = Wi sqrt(Pr/Ra) with Ra, Pr, beta fixed): Wi enters the
 // polymeric coefficient (1-beta)/(Re Wi) and the relaxation factor exp(-dt/Wi).
 //
 // The reference has no adjoint; this file is this library's own.
@@ -48,6 +52,7 @@ namespace vebi {
 void vebi_set_error_text(const std::string& msg);
 void launch_bicgstab_on(Ctx& x, const BiArgs& a, bool nonull);
 void launch_ppe_mg(Ctx& x);
+void launch_ppe_mixed_solve(Ctx& x);
 
 namespace {
 
@@ -171,6 +176,35 @@ __global__ void k_adj_mirror_coefs(Consts c, Dev d, const double* __restrict__ g
     }
     irel_out[m] = i;
   }
+}
+
+// a mixed-precision step's FP32 weights and correction matrices, widened into tape slot t
+__global__ void k_adj_widen(Dev d, Tape t, long long ell, int n) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < ell; e += stride) {
+    t.wgx[e] = (double)d.wGx32[e];
+    t.wgy[e] = (double)d.wGy32[e];
+    t.wl[e] = (double)d.wL32[e];
+  }
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    for (int q = 0; q < 4; ++q) t.kg[q][i] = (double)d.kgcm32[q][i];
+}
+
+// A^T for the mixed solver: its values in FP32 and its FP64 row sums (diagonal first, then the
+// slots in order, as the forward assembly sums A's), for the SpMV's difference form
+__global__ void k_adj_at32(int n, const int* __restrict__ acnt, const double* __restrict__ aval,
+                           const double* __restrict__ pdiag, float* __restrict__ aval32,
+                           double* __restrict__ arow) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double rs = pdiag[i];
+  const int cnt = acnt[i];
+  for (int k = 0; k < cnt; ++k) {
+    const double v = aval[(size_t)k * n + i];
+    rs += v;
+    aval32[(size_t)k * n + i] = (float)v;
+  }
+  arow[i] = rs;
 }
 
 // ------------------------------------------------------------------ counting-sort transposes
@@ -676,6 +710,8 @@ struct Adjoint {
   Trans T{};
   AdjVec a{};
   double* sums = nullptr;   // per step: dJ/dcp, dJ/de1
+  float* aval32 = nullptr;  // mixed contexts: A^T in FP32 (same slots as Trans::aval)
+  double* arow = nullptr;   // mixed contexts: A^T's row sums
   double* tmp1 = nullptr;
   std::vector<void*> allocs;
   int ls_iters_total = 0;
@@ -704,7 +740,8 @@ int adjoint_check_scope(const Ctx& x) {
   if (c.const_mod != 1 && c.eps_ptt != 0.0) return afail(VEBI_ERR_ARG, "adjoint: Oldroyd-B (ve_nonlinearity = 0) only");
   if (c.correct_velocity) return afail(VEBI_ERR_ARG, "adjoint: correct_velocity is not supported");
   if (c.warm_start) return afail(VEBI_ERR_ARG, "adjoint: the PPE warm start is not supported");
-  if (x.precision != VEBI_PREC_FP64) return afail(VEBI_ERR_ARG, "adjoint: FP64 contexts only");
+  if (x.precision != VEBI_PREC_FP64 && x.precision != VEBI_PREC_MIXED)
+    return afail(VEBI_ERR_ARG, "adjoint: FP64 or mixed-precision contexts only");
   if (c.npfb >= (1 << (31 - SLOT_BITS))) return afail(VEBI_ERR_ARG, "adjoint: too many particles");
   if (c.nplink > (1 << SLOT_BITS)) return afail(VEBI_ERR_ARG, "adjoint: nplink above 128");
   return VEBI_OK;
@@ -793,6 +830,10 @@ int adjoint_create(Ctx& x, int max_steps, int K, Adjoint** out) {
   a.mth = aalloc<double>(*A, mcap, err);
   a.part = aalloc<double>(*A, n / TPB + 2, err);
   A->sums = aalloc<double>(*A, 2 * (size_t)max_steps + 2, err);
+  if (x.precision == VEBI_PREC_MIXED) {
+    A->aval32 = aalloc<float>(*A, (size_t)T.capT * n, err);
+    A->arow = aalloc<double>(*A, n, err);
+  }
   A->tmp1 = aalloc<double>(*A, 4, err);
   if (err != cudaSuccess) {
     for (void* p : A->allocs) cudaFree(p);
@@ -877,7 +918,6 @@ static int tape_step(Adjoint& A, int s, Tape& t) {
   int rc = run_one_step(x, &st);
   x.rep_geo = nullptr;
   if (rc) return rc;
-  A.ls_iters_total += st.LS_iters;
   t.nm = st.nmirror;
   t.kmax = st.maxneighbours < (int)A.kp ? st.maxneighbours : (int)A.kp;
   t.dt = st.dt;
@@ -885,14 +925,23 @@ static int tape_step(Adjoint& A, int s, Tape& t) {
   cudaMemcpyAsync(t.cnt, x.d.ij_count, sizeof(int) * n, cudaMemcpyDeviceToDevice, x.st);
   cudaMemcpyAsync(t.link, x.d.ij_link, sizeof(int) * ell, cudaMemcpyDeviceToDevice, x.st);
   cudaMemcpyAsync(t.pcol, x.d.ppe_col, sizeof(int) * ell, cudaMemcpyDeviceToDevice, x.st);
-  cudaMemcpyAsync(t.wgx, x.d.wGx, sizeof(double) * ell, cudaMemcpyDeviceToDevice, x.st);
-  cudaMemcpyAsync(t.wgy, x.d.wGy, sizeof(double) * ell, cudaMemcpyDeviceToDevice, x.st);
-  cudaMemcpyAsync(t.wl, x.d.wL, sizeof(double) * ell, cudaMemcpyDeviceToDevice, x.st);
+  const bool mixed = x.precision == VEBI_PREC_MIXED;
+  if (mixed) {  // the FP32 weights and correction matrices the step used (the FP64 ones are not computed)
+    const long long ecount = (long long)ell;
+    const int g = grid_for(ecount > (long long)n ? ecount : (long long)n);
+    k_adj_widen<<<g < 4096 ? g : 4096, TPB, 0, x.st>>>(x.d, t, ecount, (int)n);
+    x.launches++;
+  } else {
+    cudaMemcpyAsync(t.wgx, x.d.wGx, sizeof(double) * ell, cudaMemcpyDeviceToDevice, x.st);
+    cudaMemcpyAsync(t.wgy, x.d.wGy, sizeof(double) * ell, cudaMemcpyDeviceToDevice, x.st);
+    cudaMemcpyAsync(t.wl, x.d.wL, sizeof(double) * ell, cudaMemcpyDeviceToDevice, x.st);
+  }
+  // the PPE matrix is FP64 in both contexts (a mixed step assembles it from its FP32 weights)
   cudaMemcpyAsync(t.pval, x.d.ppe_val, sizeof(double) * ell, cudaMemcpyDeviceToDevice, x.st);
   cudaMemcpyAsync(t.pdiag, x.d.ppe_diag, B, cudaMemcpyDeviceToDevice, x.st);
   const size_t np = n + (size_t)t.nm;
   for (int q = 0; q < 4; ++q) {
-    cudaMemcpyAsync(t.kg[q], x.d.kgcm[q], B, cudaMemcpyDeviceToDevice, x.st);
+    if (!mixed) cudaMemcpyAsync(t.kg[q], x.d.kgcm[q], B, cudaMemcpyDeviceToDevice, x.st);
     cudaMemcpyAsync(t.G[q], x.d.grad[q], B, cudaMemcpyDeviceToDevice, x.st);
     cudaMemcpyAsync(t.tau1[q], x.d.tau[q], sizeof(double) * np, cudaMemcpyDeviceToDevice, x.st);
   }
@@ -976,7 +1025,23 @@ static int vjp_step(Adjoint& A, int s, const Tape& t) {
   k_adj_final_sum<<<1, TPB, 0, x.st>>>(g, a.part, A.tmp1 + 1);
   k_adj_scale<<<g, TPB, 0, x.st>>>(n, A.tmp1 + 1, a.aP, 1);
   x.launches += 6;
-  if (c.precond) {
+  if (x.precision == VEBI_PREC_MIXED) {
+    // the context's own mixed solver (FP64 recurrences, FP32 SpMV in the difference form, with
+    // or without its multigrid) on A^T: FP32 values and FP64 row sums of A^T first
+    k_adj_at32<<<g, TPB, 0, x.st>>>(n, T.acnt, T.aval, t.pdiag, A.aval32, A.arow);
+    x.launches++;
+    Dev keep = x.d;
+    x.d.ppe_col = T.acol;
+    x.d.ppe_val = T.aval;
+    x.d.ppe_val32 = A.aval32;
+    x.d.rowsum = A.arow;
+    x.d.ij_count = T.acnt;
+    x.d.ppe_diag = t.pdiag;
+    x.d.ppe_B = a.aP;
+    x.d.p = a.lam;
+    launch_ppe_mixed_solve(x);
+    x.d = keep;
+  } else if (c.precond) {
     // the context's multigrid on A^T: the same set-up and solver read the transposed arrays
     // (piecewise-constant aggregation: the Galerkin levels of A^T are those of A transposed)
     Dev keep = x.d;
