@@ -422,7 +422,7 @@ def run_adjoint(args, dist: Dist) -> dict:
               else "the reference's PPE solver")
     model = "Oldroyd-B Wi=0.5 beta=0.5" if case.const_mod != 1 else "Newtonian (const_mod 1) beta=0.5"
     step = ("mixed-precision step (FP32 pair sums and SpMV; the VJP in FP64 on its widened weights, "
-            "the transposed solve in FP64)" if mixed else "FP64 step")
+            "the transposed solve by the context's mixed solver)" if mixed else "FP64 step")
     return {"workload": f"{case.name}: heated cavity, {n - nbS} fluid + {nbS} wall particles, Ra=1e5 Pr=1 "
                         f"{model}, {step}, {solver}, PPE tol {case.tol:g}, {args.adjoint_spinup} steps "
                         f"of spin-up",

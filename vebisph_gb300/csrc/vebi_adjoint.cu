@@ -20,7 +20,8 @@
 //   right-hand side   b_i = -(1/dt) sum_k (u*_i - u*_j).(K_i gradW_ik), mean removed
 //   predictor         u* = u + dt (cp (tau_j - tau_i).(K_i gradW) + cs (u_i - u_j) wL) + buoyancy,
 //                     theta* = theta + dt ct sum (theta_i - theta_j) wL
-//   log-conformation  per particle, Jacobian in forward mode (vebi_adjoint_logconf.cuh)
+//   log-conformation  per particle, three small forward-mode Jacobians chained backwards
+//                     (vebi_adjoint_logconf.cuh)
 //   gradients         grad u_i = K_i sum_k (u_j - u_i) gradW_ik
 // and the mirror transfers (creation values, mirror velocities, mirror stress, mirror pressure)
 // through their linear parts.  The j-side of every pair sum is gathered, not scattered: a
@@ -262,20 +263,67 @@ __global__ void k_adj_fill_cols(int npfb, const int* __restrict__ cnt, const int
     aent[aptr[col] + atomicAdd(&afill[col], 1)] = (i << SLOT_BITS) | k;
   }
 }
-// sort every segment ascending (insertion sort: segments hold tens of entries)
-__global__ void k_adj_sort_segments(int n, const int* __restrict__ ptr, int* __restrict__ ent) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  const int a = ptr[s], b = ptr[s + 1];
-  for (int q = a + 1; q < b; ++q) {
-    const int v = ent[q];
-    int r = q - 1;
-    while (r >= a && ent[r] > v) {
-      ent[r + 1] = ent[r];
-      --r;
-    }
-    ent[r + 1] = v;
+// Sort every segment ascending.  One warp per segment: each lane holds up to R of its entries
+// in registers, every entry's rank is the number of entries below it (the entries of a segment
+// are distinct: (row, slot) codes or mirror indices), and each entry is stored at its rank.
+// Segments of up to 64 entries (nearly all) take R = 2, up to 256 R = 8; a longer one (none with
+// nplink <= 128) is sorted by one lane.
+template <int R>
+__device__ __forceinline__ void warp_rank_sort(int* __restrict__ ent, int a, int len, int lane) {
+  int v[R], rk[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const int e = lane + 32 * q;
+    v[q] = e < len ? ent[a + e] : 0x7fffffff;
+    rk[q] = 0;
   }
+#pragma unroll
+  for (int q2 = 0; q2 < R; ++q2) {
+    if (32 * q2 >= len) break;
+    for (int src = 0; src < 32; ++src) {
+      const int o = __shfl_sync(0xffffffffu, v[q2], src);
+#pragma unroll
+      for (int q = 0; q < R; ++q) rk[q] += (o < v[q]) ? 1 : 0;
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const int e = lane + 32 * q;
+    if (e < len) ent[a + rk[q]] = v[q];
+  }
+  __syncwarp();
+}
+__global__ void k_adj_sort_segments(int n, const int* __restrict__ ptr, int* __restrict__ ent) {
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < n; s += nw) {
+    const int a = ptr[s], len = ptr[s + 1] - a;
+    if (len <= 1) continue;
+    if (len <= 64) {
+      warp_rank_sort<2>(ent, a, len, lane);
+    } else if (len <= 256) {
+      warp_rank_sort<8>(ent, a, len, lane);
+    } else {
+      if (lane == 0) {
+        for (int q = a + 1; q < a + len; ++q) {
+          const int v = ent[q];
+          int r = q - 1;
+          while (r >= a && ent[r] > v) {
+            ent[r + 1] = ent[r];
+            --r;
+          }
+          ent[r + 1] = v;
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+static int sort_grid(int segments) {
+  const long long warps = segments > 0 ? segments : 1;
+  const long long g = (warps * 32 + TPB - 1) / TPB;
+  return (int)(g < 4096 ? g : 4096);
 }
 // A^T in the ELL layout of the step's solver: row c of A^T lists (i, A_ic) in ascending i
 __global__ void k_adj_write_at(int npfb, int capT, const int* __restrict__ aptr, const int* __restrict__ aent,
@@ -516,9 +564,7 @@ __global__ void k_adj_gather_us(Consts c, Tape t, Trans T, AdjVec a, int np) {
 
 // predictor, own-row part; dJ/dcp of this step into part
 __global__ void k_adj_pred_rows(Consts c, Tape t, AdjVec a, int ve) {
-  __shared__ double sh[TPB / 32 + 1];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double dcp = 0.0;
   if (i < c.npfb) {
     const double us = a.aus[i], vs = a.avs[i], ths = a.Rth[i];
     a.Nu[i] += us;
@@ -538,9 +584,6 @@ __global__ void k_adj_pred_rows(Consts c, Tape t, AdjVec a, int ve) {
     const double K11 = t.kg[0][i], K21 = t.kg[1][i], K12 = t.kg[2][i], K22 = t.kg[3][i];
     double swl = 0.0, o0 = 0.0, o1 = 0.0, o2 = 0.0, o3 = 0.0;
     const int cnt = t.cnt[i];
-    double Ti[4] = {0.0, 0.0, 0.0, 0.0};
-    if (ve)
-      for (int q = 0; q < 4; ++q) Ti[q] = t.tau1[q][i];
     for (int k = 0; k < cnt; ++k) {
       const size_t e = (size_t)k * c.npfb + i;
       swl += t.wl[e];
@@ -551,10 +594,6 @@ __global__ void k_adj_pred_rows(Consts c, Tape t, AdjVec a, int ve) {
         o2 -= cp * kw2 * s1;
         o1 -= cp * kw1 * s2;
         o3 -= cp * kw2 * s2;
-        const int j = t.link[e];
-        const double T11 = t.tau1[0][j] - Ti[0], T21 = t.tau1[1][j] - Ti[1];
-        const double T12 = t.tau1[2][j] - Ti[2], T22 = t.tau1[3][j] - Ti[3];
-        dcp += s1 * (T11 * kw1 + T12 * kw2) + s2 * (T21 * kw1 + T22 * kw2);
       }
     }
     a.Nu[i] += cs * s1 * swl;
@@ -565,8 +604,6 @@ __global__ void k_adj_pred_rows(Consts c, Tape t, AdjVec a, int ve) {
     a.at[2][i] = o2;
     a.at[3][i] = o3;
   }
-  dcp = block_sum<TPB>(dcp, sh);
-  if (threadIdx.x == 0) a.part[blockIdx.x] = dcp;
 }
 __global__ void k_adj_gather_pred(Consts c, Tape t, Trans T, AdjVec a, int np, int ve) {
   const int cc = blockIdx.x * blockDim.x + threadIdx.x;
@@ -610,6 +647,25 @@ __global__ void k_adj_gather_pred(Consts c, Tape t, Trans T, AdjVec a, int np, i
   }
 }
 
+// dJ/dcp of this step into part: the polymeric pair sum is bilinear in cp and tau, so
+// cp dJ/dcp = sum over particles and mirrors of tau . tau-bar (its own-row and gathered parts,
+// before the mirrors' share moves to the parents), with no second pass over the pairs.
+// A grid-stride loop over np; one partial per block (grid <= npfb / TPB + 1 blocks).
+__global__ void k_adj_dcp(Consts c, Tape t, AdjVec a, int np, double inv_cp) {
+  __shared__ double sh[TPB / 32 + 1];
+  double acc = 0.0;
+  for (int cc = blockIdx.x * blockDim.x + threadIdx.x; cc < np; cc += gridDim.x * blockDim.x) {
+    if (cc < c.npfb) {
+      for (int q = 0; q < 4; ++q) acc += t.tau1[q][cc] * a.at[q][cc];
+    } else {
+      const int m = cc - c.npfb;
+      for (int q = 0; q < 4; ++q) acc += t.tau1[q][cc] * a.mt[q][m];
+    }
+  }
+  acc = block_sum<TPB>(acc, sh);
+  if (threadIdx.x == 0) a.part[blockIdx.x] = acc * inv_cp;
+}
+
 // log-conformation: (tau-bar^n, G-bar) = J^T tau-bar^{n+1}; dJ/de1 of this step into part
 __global__ void k_adj_logconf(Consts c, Tape t, AdjVec a, double e1, int ve) {
   __shared__ double sh[TPB / 32 + 1];
@@ -619,25 +675,17 @@ __global__ void k_adj_logconf(Consts c, Tape t, AdjVec a, double e1, int ve) {
     double tb[4];
     for (int q = 0; q < 4; ++q) tb[q] = a.Rtau[q][i] + a.at[q][i];
     if (ve) {
-      Dual9 tau[4], G[4], out[4];
+      double tau[4], G[4], taub[4], Gb[4], e1b;
       for (int q = 0; q < 4; ++q) {
-        tau[q] = Dual9(t.tau0[q][i]);
-        tau[q].d[q] = 1.0;
-        G[q] = Dual9(t.G[q][i]);
-        G[q].d[4 + q] = 1.0;
+        tau[q] = t.tau0[q][i];
+        G[q] = t.G[q][i];
       }
-      Dual9 e(e1);
-      e.d[8] = 1.0;
-      logconf_eval<Dual9>(tau, G, t.dt, e, out);
+      logconf_vjp(tau, G, t.dt, e1, tb, taub, Gb, e1b);
       for (int q = 0; q < 4; ++q) {
-        double s = 0.0;
-        for (int r = 0; r < 4; ++r) s += out[r].d[q] * tb[r];
-        a.Ntau[q][i] += s;
-        double g = 0.0;
-        for (int r = 0; r < 4; ++r) g += out[r].d[4 + q] * tb[r];
-        a.Gb[q][i] = g;
+        a.Ntau[q][i] += taub[q];
+        a.Gb[q][i] = Gb[q];
       }
-      for (int r = 0; r < 4; ++r) de1 += out[r].d[8] * tb[r];
+      de1 += e1b;
     } else {  // Newtonian: tau is carried unchanged
       for (int q = 0; q < 4; ++q) {
         a.Ntau[q][i] += tb[q];
@@ -970,19 +1018,19 @@ static void build_transposes(Adjoint& A, const Tape& t) {
   scan_into(x, np, T.tfill, T.tptr, T.scan_tot);
   cudaMemsetAsync(T.tfill, 0, sizeof(int) * np, x.st);
   k_adj_fill_pairs<<<grid_for(n), TPB, 0, x.st>>>(n, t.cnt, t.link, T.tptr, T.tfill, T.tent);
-  k_adj_sort_segments<<<grid_for(np), TPB, 0, x.st>>>(np, T.tptr, T.tent);
+  k_adj_sort_segments<<<sort_grid(np), TPB, 0, x.st>>>(np, T.tptr, T.tent);
   cudaMemsetAsync(T.mfill, 0, sizeof(int) * n, x.st);
   if (t.nm > 0) k_adj_count_mirrors<<<grid_for(t.nm), TPB, 0, x.st>>>(t.nm, t.irel, T.mfill);
   scan_into(x, n, T.mfill, T.mptr, T.scan_tot);
   cudaMemsetAsync(T.mfill, 0, sizeof(int) * n, x.st);
   if (t.nm > 0) k_adj_fill_mirrors<<<grid_for(t.nm), TPB, 0, x.st>>>(t.nm, t.irel, T.mptr, T.mfill, T.ment);
-  k_adj_sort_segments<<<grid_for(n), TPB, 0, x.st>>>(n, T.mptr, T.ment);
+  k_adj_sort_segments<<<sort_grid(n), TPB, 0, x.st>>>(n, T.mptr, T.ment);
   cudaMemsetAsync(T.afill, 0, sizeof(int) * n, x.st);
   k_adj_count_cols<<<grid_for(n), TPB, 0, x.st>>>(n, t.cnt, t.pcol, t.pval, T.afill);
   scan_into(x, n, T.afill, T.aptr, T.scan_tot);
   cudaMemsetAsync(T.afill, 0, sizeof(int) * n, x.st);
   k_adj_fill_cols<<<grid_for(n), TPB, 0, x.st>>>(n, t.cnt, t.pcol, t.pval, T.aptr, T.afill, T.aent);
-  k_adj_sort_segments<<<grid_for(n), TPB, 0, x.st>>>(n, T.aptr, T.aent);
+  k_adj_sort_segments<<<sort_grid(n), TPB, 0, x.st>>>(n, T.aptr, T.aent);
   k_adj_write_at<<<grid_for(n), TPB, 0, x.st>>>(n, T.capT, T.aptr, T.aent, t.pval, T.acnt, T.acol, T.aval, T.flag);
   x.launches += 10 + (t.nm > 0 ? 2 : 0);
 }
@@ -1068,8 +1116,13 @@ static int vjp_step(Adjoint& A, int s, const Tape& t) {
   k_adj_push<<<g, TPB, 0, x.st>>>(c, T, t.mco, 2, a.aus, 1, a.aus, a.avs, a.avs);
   // predictor
   k_adj_pred_rows<<<g, TPB, 0, x.st>>>(c, t, a, ve);
-  k_adj_final_sum<<<1, TPB, 0, x.st>>>(g, a.part, A.sums + 2 * (size_t)s);
   k_adj_gather_pred<<<gp, TPB, 0, x.st>>>(c, t, T, a, np, ve);
+  if (ve) {
+    const double inv_cp = c.coeff_polymeric != 0.0 ? 1.0 / c.coeff_polymeric : 0.0;
+    k_adj_dcp<<<g, TPB, 0, x.st>>>(c, t, a, np, inv_cp);
+    k_adj_final_sum<<<1, TPB, 0, x.st>>>(g, a.part, A.sums + 2 * (size_t)s);
+    x.launches += 2;
+  }
   k_adj_push<<<g, TPB, 0, x.st>>>(c, T, t.mco, 0, a.mu, 0, a.Nu, a.mv, a.Nv);
   k_adj_push<<<g, TPB, 0, x.st>>>(c, T, t.mco, 1, a.mth, 0, a.Nth, nullptr, nullptr);
   if (ve) k_adj_push_tau<<<g, TPB, 0, x.st>>>(c, T, t.mco, a);
@@ -1082,7 +1135,7 @@ static int vjp_step(Adjoint& A, int s, const Tape& t) {
     k_adj_gather_grad<<<gp, TPB, 0, x.st>>>(c, t, T, a, np);
     k_adj_push<<<g, TPB, 0, x.st>>>(c, T, t.mco, 0, a.mu, 0, a.Nu, a.mv, a.Nv);
   }
-  x.launches += 12;
+  x.launches += 11;
   // state adjoint of step s
   std::swap(a.Ru, a.Nu);
   std::swap(a.Rv, a.Nv);
