@@ -27,6 +27,13 @@
 //
 // Indexing: 0-based.  Particle i here is particle i+1 of the reference.  Integer codes
 // (vrelation, b_periodic_parent) keep the reference's 1-based patch numbers.
+//
+// Tangent-linear model.  The step is written once over the scalar type of its fields
+// (OracleT<R>): OracleT<double> is the restatement; OracleT<Tan> runs the same code over
+// forward-mode dual numbers (orc_tlm_*), giving the FP64 tangent-linear model of the step with
+// the geometry (positions, dt, pair lists, weights, PPE matrix) of the unperturbed trajectory.
+// It is the reference gradient the GPU adjoint is checked against.  orc_geometry records and
+// replays r* and dt of an FP64 run, so that central differences see the same map.
 
 #include "../include/vebi.h"
 
