@@ -134,3 +134,29 @@ def test_cylinder_tangent_matches_central_differences(const_mod):
     tl, _ = w.tangent("u", d)
     fd = w.central("u", d, 1.0e-4)
     assert abs(fd - tl) <= 1.0e-8 * abs(fd), (fd, tl)
+
+
+@pytest.mark.parametrize("field,eps,rtol", [("theta", 1.0e-3, 1.0e-8), ("tau", 1.0e-4, 1.0e-8)])
+def test_ptt_cavity_tangent_matches_central_differences(field, eps, rtol):
+    """PTT (ve_nonlinearity 0.25): the relaxation rate follows the conformation's trace."""
+    case = cases.cavity(n=16, seed=3, Ra=1.0e4, Wi=0.5, beta=0.5, amp=2.0e-2)
+    case.ve_nonlinearity = 0.25
+    w = Window(case)
+    d = w.direction(field, 40)
+    tl, j = w.tangent(field, d)
+    assert j == w.J0
+    fd = w.central(field, d, eps)
+    assert abs(fd - tl) <= rtol * abs(fd), (fd, tl)
+
+
+@pytest.mark.parametrize("make,rtol", [(lambda: cases.dam_break(20, seed=1), 1.0e-8),
+                                       (lambda: cases.free_surface_periodic(30, seed=1), 1.0e-6)])
+def test_open_domain_tangent_matches_central_differences(make, rtol):
+    """Open domains: free-surface Dirichlet rows, the smoothed PPE and the Jacobi BiCGSTAB (the
+    dam break under gravity; the periodic free-surface layer), step 1e-3."""
+    w = Window(make())
+    d = w.direction("u", 40)
+    tl, j = w.tangent("u", d)
+    assert j == w.J0
+    fd = w.central("u", d, 1.0e-3)
+    assert abs(fd - tl) <= rtol * abs(fd), (fd, tl)
