@@ -161,7 +161,9 @@ class Adjoint:
     record(n) runs n ordinary steps from the solver's state and keeps their geometry (advected
     positions, dt) and the fields every `checkpoint_every` steps; replay(n) runs the
     differentiated map -- the same steps with the recorded geometry -- from the solver's current
-    fields; reverse(...) returns dJ/d(state before the window) from dJ/d(state after it)."""
+    fields; reverse(...) returns dJ/d(state before the window) from dJ/d(state after it).
+    The solver may be FP64 or mixed-precision: a mixed window runs the mixed step, and its
+    reverse sweep differentiates the mixed map in FP64 with the FP32 weights the steps used."""
 
     def __init__(self, solver: StepSolver, max_steps: int, checkpoint_every: int = 20):
         self.solver = solver
