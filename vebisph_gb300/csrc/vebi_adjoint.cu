@@ -35,8 +35,9 @@
 // matrices, FP32 pair sums); the tape widens the step's FP32 weights and correction matrices to
 // FP64, so the VJP, in FP64, is that of the mixed map with the weights it used, exact up to the
 // FP32 rounding of its pair sums; the transposed solve runs the context's mixed solver (FP64
-// recurrences, FP32 SpMV) on an FP32 copy of A^T.  The adjoint also returns dJ/dWi (El = Wi sqrt(Pr/Ra) with Ra, Pr, beta fixed): Wi enters the
-// polymeric coefficient (1-beta)/(Re Wi) and the relaxation factor exp(-dt/Wi).
+// recurrences, FP32 SpMV) on an FP32 copy of A^T.  The adjoint also returns dJ/dWi
+// (El = Wi sqrt(Pr/Ra) with Ra, Pr, beta fixed): Wi enters the polymeric coefficient
+// (1-beta)/(Re Wi) and the relaxation factor exp(-dt/Wi).
 //
 // The reference has no adjoint; this file is this library's own.
 #include <algorithm>
