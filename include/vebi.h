@@ -278,15 +278,17 @@ const char* vebi_last_error(void);
  * and dt -- taken from the recorded base trajectory.
  *
  * vebi_adjoint_record runs nsteps ordinary steps from the context's state, keeping every step's
- * geometry and the fields every checkpoint_every steps.  vebi_adjoint_replay runs the
+ * geometry and pressure (24 bytes per particle per step) and the fields every checkpoint_every
+ * steps.  vebi_adjoint_replay runs the
  * differentiated map itself from the context's current fields (upload a perturbed state first:
  * finite differences go through it); replaying the unperturbed state reproduces the record.
  * vebi_adjoint_restore puts a checkpointed state back into the context.  vebi_adjoint_reverse
  * takes dJ/d(state after the window) -- seed_u (2 planes), seed_theta, seed_tau (4 planes),
  * leading dimension ld, any of them NULL for zero -- and returns dJ/d(state before the window)
  * in the same layout, dJ/dWi (Ra, Pr, beta fixed), and the transposed BiCGSTAB iterations.
- * It replays each segment from its checkpoint to rebuild the steps' intermediates, so it leaves
- * the context's fields at an intermediate state.
+ * It replays each segment from its checkpoint to rebuild the steps' intermediates, taking each
+ * step's pressure from the record instead of solving the PPE again, so it leaves the context's
+ * fields at an intermediate state.
  *
  * Scope: closed domains with wall and periodic patches (and their corners) and circles,
  * Newtonian or Oldroyd-B (ve_nonlinearity = 0), FP64 or mixed-precision contexts, no PPE warm

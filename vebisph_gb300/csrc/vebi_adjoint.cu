@@ -8,9 +8,10 @@
 // (vebi_adjoint_replay runs that map, so finite differences see the same function).  The
 // position update of the fields' next step is not differentiated.
 //
-// Reverse sweep.  The record run keeps the geometry (r*, dt) of every step and the fields every
-// K steps.  The reverse sweep walks the checkpoints backwards: it restores one, replays its K
-// steps forward while copying into a tape what the step's VJP needs (pair list and weights,
+// Reverse sweep.  The record run keeps the geometry (r*, dt) and the pressure of every step and
+// the fields every K steps.  The reverse sweep walks the checkpoints backwards: it restores one,
+// replays its K steps forward -- taking each step's pressure from the record instead of solving
+// the PPE again -- while copying into a tape what the step's VJP needs (pair list and weights,
 // correction matrices, PPE matrix, velocity gradients, tau before and after, per-mirror
 // transfer coefficients), then runs the VJP kernels from the last of those steps to the first.
 // The VJP of one step, in reverse order of the forward stages:
@@ -753,6 +754,7 @@ struct Adjoint {
   int max_steps = 0, K = 1, nsteps = 0, nseg = 0;
   size_t n = 0, cap = 0, mcap = 0, kp = 0;
   double* geo = nullptr;    // per step: r* x, r* y (npfb each), dt
+  double* pres = nullptr;   // per step: the pressure P (npfb)
   double* ckpt = nullptr;   // per checkpoint: u, v, theta, tau x4, trace, r x, r y (npfb each)
   uint8_t* ckpt_inbin = nullptr;
   std::vector<Tape> tape;   // K slots
@@ -813,6 +815,7 @@ int adjoint_create(Ctx& x, int max_steps, int K, Adjoint** out) {
   const int nck = (max_steps + A->K - 1) / A->K;
   cudaError_t err = cudaSuccess;
   A->geo = aalloc<double>(*A, (size_t)max_steps * (2 * n + 1), err);
+  A->pres = aalloc<double>(*A, (size_t)max_steps * n, err);
   A->ckpt = aalloc<double>(*A, (size_t)nck * CK_PLANES * n, err);
   A->ckpt_inbin = aalloc<uint8_t>(*A, (size_t)nck * n, err);
   A->tape.resize(A->K);
@@ -932,6 +935,7 @@ int adjoint_record(Adjoint& A, int nsteps, vebi_step_stats* last) {
     const int st = run_one_step(x, last);
     x.rec_geo = nullptr;
     if (st) return st;
+    cudaMemcpyAsync(A.pres + (size_t)s * A.n, x.d.p, sizeof(double) * A.n, cudaMemcpyDeviceToDevice, x.st);
   }
   A.nsteps = nsteps;
   return VEBI_OK;
@@ -964,8 +968,10 @@ static int tape_step(Adjoint& A, int s, Tape& t) {
   vebi_step_stats st{};
   const double* geo = A.geo + (size_t)s * (2 * A.n + 1);
   x.rep_geo = geo;
+  x.rep_p = A.pres + (size_t)s * n;
   int rc = run_one_step(x, &st);
   x.rep_geo = nullptr;
+  x.rep_p = nullptr;
   if (rc) return rc;
   t.nm = st.nmirror;
   t.kmax = st.maxneighbours < (int)A.kp ? st.maxneighbours : (int)A.kp;

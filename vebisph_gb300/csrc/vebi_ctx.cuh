@@ -51,6 +51,9 @@ struct Ctx {
   // them from rep_geo instead of its own, so that it replays a recorded step's geometry
   double* rec_geo = nullptr;
   const double* rep_geo = nullptr;
+  // adjoint: when set, the step takes its pressure (npfb values) from rep_p instead of solving
+  // the PPE; the reverse sweep's recompute of a recorded step, whose solution is known
+  const double* rep_p = nullptr;
   vebi_step_stats last{};
 };
 

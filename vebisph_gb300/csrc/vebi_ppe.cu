@@ -311,6 +311,10 @@ void launch_ppe(Ctx& x) {
   VEBI_LAUNCH(x, k_ppe_mean, 1, TPB, c, x.d, g);
   VEBI_LAUNCH(x, k_ppe_assemble, g, TPB, c, x.d, mixed ? (const float*)x.d.wL32 : (const float*)nullptr);
   stage_mark(x, 10);
+  if (x.rep_p) {  // a recorded step recomputed by the adjoint: its solution is known
+    cudaMemcpyAsync(x.d.p, x.rep_p, sizeof(double) * (size_t)c.npfb, cudaMemcpyDeviceToDevice, x.st);
+    return;
+  }
   if (x.precision == VEBI_PREC_MIXED) {
     launch_ppe_mixed_solve(x);
     return;
