@@ -45,3 +45,18 @@ def test_record_kinds(lib):
     assert lib.vebi_format_list(None, None, None, buf, 256) == -1
     n = lib.vebi_format_list(b"", None, None, buf, 256)
     assert n == 1 and buf.value == b"\n"
+
+
+def test_adjoint_arguments(lib):
+    """The adjoint's entry points reject null handles, and the Weissenberg setter a null context
+    or a non-positive value, before any device work."""
+    a = C.c_void_p()
+    assert lib.vebi_adjoint_create(None, 4, 2, C.byref(a)) == 1
+    assert lib.vebi_adjoint_create(None, 4, 2, None) == 1
+    assert lib.vebi_adjoint_record(None, 1, None) == 1
+    assert lib.vebi_adjoint_replay(None, 1, None) == 1
+    assert lib.vebi_adjoint_restore(None, 0) == 1
+    assert lib.vebi_adjoint_reverse(None, None, None, None, 1, None, None, None, None, None) == 1
+    assert b"adjoint" in lib.vebi_last_error()
+    assert lib.vebi_adjoint_destroy(None) == 0
+    assert lib.vebi_set_weissenberg(None, 0.5) == 1
