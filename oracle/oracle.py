@@ -50,6 +50,8 @@ def load():
         lib.orc_tlm_get.argtypes = [vp, C.c_char_p, P(C.c_double), P(C.c_double), C.c_int64]
         lib.orc_tlm_set_itermax.argtypes = [vp, C.c_int]
         lib.orc_tlm_box.argtypes = [vp, P(C.c_double)]
+        lib.orc_logconf_particle.argtypes = [P(C.c_double), P(C.c_double), P(C.c_double), C.c_double,
+                                             C.c_double, C.c_double, C.c_int]
         _lib = lib
     return _lib
 
@@ -224,6 +226,18 @@ class TangentLinear:
             self.close()
         except Exception:
             pass
+
+
+def logconf_particle(tau, grad_u, dt, Wi, eps_ptt=0.0, nsteps=1, trace=None):
+    """nsteps of one particle's log-conformation update (constitutive_eqn_evolve) under a fixed
+    velocity gradient: tau = (t11, t21, t12, t22), grad_u = (du/dx, du/dy, dv/dx, dv/dy).
+    Returns the stress and the conformation trace after them."""
+    lib = load()
+    t = np.ascontiguousarray(np.asarray(tau, float).ravel().copy())
+    g = np.ascontiguousarray(np.asarray(grad_u, float).ravel())
+    tr = C.c_double(2.0 + t[0] + t[3] if trace is None else float(trace))
+    lib.orc_logconf_particle(_dp(t), C.byref(tr), _dp(g), float(dt), float(Wi), float(eps_ptt), int(nsteps))
+    return t, tr.value
 
 
 def eigens(A):

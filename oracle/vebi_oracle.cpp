@@ -1150,52 +1150,62 @@ struct OracleT {
     Q.a21.d = A.a21.d / gap;
     Q.a12.d = -Q.a21.d;
   }
-  // constitutive_eqn_evolve (predictor_mod.F90:141-251), Lagrangian, const_mod=2
+  // constitutive_eqn_evolve (predictor_mod.F90:141-251), Lagrangian, const_mod=2: the update
+  // of one particle's stress t (planes t11, t21, t12, t22) and conformation trace under the
+  // velocity gradient g (du/dx, du/dy, dv/dx, dv/dy) over dt
+  template <class T>
+  static void logconf_particle(T t[4], T& trace, const T g[4], double dtl, double Wi, double eps_PTT) {
+    using MR = M2T<T>;
+    // steps 1-2
+    MR A{t[0] / 1.0 + 1.0, t[2] / 1.0 + 0.0, t[1] / 1.0 + 0.0, t[3] / 1.0 + 1.0};
+    A = MR{A.a11 / 1.0, A.a12 / 1.0, A.a21 / 1.0, A.a22 / 1.0};
+    T L1, L2; MR Q;
+    calc_eigens(A, L1, L2, Q);
+    // step 3
+    MR D{Log(L1), 0.0, 0.0, Log(L2)};
+    MR Psi0 = mm(Q, mm(D, tr(Q)));
+    // step 5
+    MR G{g[0], g[1], g[2], g[3]};  // G(a,b) = du_a/dx_b
+    MR tm = mm(tr(Q), mm(G, Q));
+    T tmp1 = (L2 * tm.a12 + L1 * tm.a21) / (L2 - L1 + 1e-10);
+    tm.a12 = 0.0; tm.a21 = 0.0;
+    MR B = mm(Q, mm(tm, tr(Q)));
+    MR W{0.0, tmp1, -tmp1, 0.0};
+    MR Om = mm(Q, mm(W, tr(Q)));
+    // step 6
+    MR OP = mm(Om, Psi0), PO = mm(Psi0, Om);
+    MR t6{2.0 * B.a11 + OP.a11 - PO.a11, 2.0 * B.a12 + OP.a12 - PO.a12,
+          2.0 * B.a21 + OP.a21 - PO.a21, 2.0 * B.a22 + OP.a22 - PO.a22};
+    MR Psi{Psi0.a11 + dtl * t6.a11, Psi0.a12 + dtl * t6.a12, Psi0.a21 + dtl * t6.a21,
+           Psi0.a22 + dtl * t6.a22};
+    // step 7
+    calc_eigens(Psi, L1, L2, Q);
+    L1 = Exp(L1); L2 = Exp(L2);
+    MR E2{L1, 0.0, 0.0, L2};
+    A = mm(Q, mm(E2, tr(Q)));
+    // step 8: f_relaxation_integrate (:318-331) with the old trace
+    T alpha_R = 1.0 + eps_PTT * (trace - 2.0);
+    T e1 = Exp(-(alpha_R * 1.0 * dtl / Wi));
+    T e2 = (1.0 - e1) / 1.0;
+    A = MR{A.a11 * e1 + e2 * 1.0, A.a12 * e1 + e2 * 0.0, A.a21 * e1 + e2 * 0.0, A.a22 * e1 + e2 * 1.0};
+    // step 9
+    trace = A.a11 + A.a22;
+    t[0] = 1.0 * (1.0 * A.a11 - 1.0);
+    t[2] = 1.0 * (1.0 * A.a12 - 0.0);
+    t[1] = 1.0 * (1.0 * A.a21 - 0.0);
+    t[3] = 1.0 * (1.0 * A.a22 - 1.0);
+  }
   void constitutive_eqn_evolve() {
     const double eps_PTT = P.ve_nonlinearity;
     const double Wi = P.El * std::sqrt(P.Ra / P.Pr);
-    using MR = M2T<R>;
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < npfb; ++i) {
-      // steps 1-2
-      MR A{tau[0][i] / 1.0 + 1.0, tau[2][i] / 1.0 + 0.0, tau[1][i] / 1.0 + 0.0, tau[3][i] / 1.0 + 1.0};
-      A = MR{A.a11 / 1.0, A.a12 / 1.0, A.a21 / 1.0, A.a22 / 1.0};
-      R L1, L2; MR Q;
-      calc_eigens(A, L1, L2, Q);
-      // step 3
-      MR D{Log(L1), 0.0, 0.0, Log(L2)};
-      MR Psi0 = mm(Q, mm(D, tr(Q)));
-      // step 5
-      MR G{grad[0][i], grad[1][i], grad[2][i], grad[3][i]};  // G(a,b) = du_a/dx_b
-      MR tm = mm(tr(Q), mm(G, Q));
-      R tmp1 = (L2 * tm.a12 + L1 * tm.a21) / (L2 - L1 + 1e-10);
-      tm.a12 = 0.0; tm.a21 = 0.0;
-      MR B = mm(Q, mm(tm, tr(Q)));
-      MR W{0.0, tmp1, -tmp1, 0.0};
-      MR Om = mm(Q, mm(W, tr(Q)));
-      // step 6
-      MR OP = mm(Om, Psi0), PO = mm(Psi0, Om);
-      MR t6{2.0 * B.a11 + OP.a11 - PO.a11, 2.0 * B.a12 + OP.a12 - PO.a12,
-            2.0 * B.a21 + OP.a21 - PO.a21, 2.0 * B.a22 + OP.a22 - PO.a22};
-      double dtl = dt;
-      MR Psi{Psi0.a11 + dtl * t6.a11, Psi0.a12 + dtl * t6.a12, Psi0.a21 + dtl * t6.a21,
-             Psi0.a22 + dtl * t6.a22};
-      // step 7
-      calc_eigens(Psi, L1, L2, Q);
-      L1 = Exp(L1); L2 = Exp(L2);
-      MR E2{L1, 0.0, 0.0, L2};
-      A = mm(Q, mm(E2, tr(Q)));
-      // step 8: f_relaxation_integrate (:318-331) with the old trace
-      R alpha_R = 1.0 + eps_PTT * (trace_conf[i] - 2.0);
-      R e1 = Exp(-(alpha_R * 1.0 * dtl / Wi));
-      R e2 = (1.0 - e1) / 1.0;
-      A = MR{A.a11 * e1 + e2 * 1.0, A.a12 * e1 + e2 * 0.0, A.a21 * e1 + e2 * 0.0, A.a22 * e1 + e2 * 1.0};
-      // step 9
-      trace_conf[i] = A.a11 + A.a22;
-      tau[0][i] = 1.0 * (1.0 * A.a11 - 1.0);
-      tau[2][i] = 1.0 * (1.0 * A.a12 - 0.0);
-      tau[1][i] = 1.0 * (1.0 * A.a21 - 0.0);
-      tau[3][i] = 1.0 * (1.0 * A.a22 - 1.0);
+      R t[4] = {tau[0][i], tau[1][i], tau[2][i], tau[3][i]};
+      const R g[4] = {grad[0][i], grad[1][i], grad[2][i], grad[3][i]};
+      R trace = trace_conf[i];
+      logconf_particle(t, trace, g, dt, Wi, eps_PTT);
+      for (int q = 0; q < 4; ++q) tau[q][i] = t[q];
+      trace_conf[i] = trace;
       a_out[i] = trace_conf[i];
     }
     mirror_polymeric_stress();
@@ -1879,6 +1889,13 @@ int orc_eigens(const double* A4, double* L2, double* R4) {
   M2 A{A4[0], A4[1], A4[2], A4[3]}, Q;
   Oracle::calc_eigens(A, L2[0], L2[1], Q);
   R4[0] = Q.a11; R4[1] = Q.a12; R4[2] = Q.a21; R4[3] = Q.a22;
+  return 0;
+}
+// one particle's log-conformation update (test of the constitutive law): tau4 (t11, t21, t12,
+// t22) and trace updated in place under the velocity gradient g4 (du/dx, du/dy, dv/dx, dv/dy)
+int orc_logconf_particle(double* tau4, double* trace, const double* g4, double dt, double Wi, double eps_ptt,
+                         int nsteps) {
+  for (int s = 0; s < nsteps; ++s) Oracle::logconf_particle(tau4, *trace, g4, dt, Wi, eps_ptt);
   return 0;
 }
 int orc_threads(void) {

@@ -6,6 +6,9 @@
 * calc_eigens reconstructs A = R diag(L) R^T (predictor_mod.F90:253-290);
 * at rest the log-conformation step equals the analytic relaxation tau*exp(-dt/Wi) (predictor_mod.F90:318-331);
 * the BiCGSTAB solution satisfies the assembled system;
+* in steady simple shear the log-conformation update converges to the Oldroyd-B relations of
+  docs/docs.tex:93-100 (A_xy = Wi g, tau_xx = 2 (Wi g)^2, tau_yy = 0) at first order in dt, and
+  from rest it stays at rest (the reference's degenerate-eigenvalue branch);
 * the oracle is deterministic for any OpenMP thread count;
 * a regression summary of one step on the shipped Rayleigh-Benard deck.
 """
@@ -18,7 +21,7 @@ import sys
 import numpy as np
 import pytest
 
-from oracle.oracle import OracleSolver, eigens
+from oracle.oracle import OracleSolver, eigens, logconf_particle
 from vebisph_gb300 import cases
 
 ROOT = pathlib.Path(__file__).resolve().parent.parent
@@ -110,6 +113,33 @@ def _ell_matvec(o, x, n):
     val = o.get("ppe_val").reshape(-1, n)[:k]
     mask = np.arange(k)[:, None] < cnt[None, :]
     return o.get("ppe_diag") * x + (np.where(mask, val, 0.0) * x[col]).sum(0)
+
+
+@pytest.mark.parametrize("Wi,g", [(1.0, 0.5), (0.5, 2.0), (2.0, 0.3)])
+def test_steady_shear_matches_oldroyd_b(Wi, g):
+    """Simple shear du/dy = g held for 30 relaxation times from a slightly anisotropic
+    conformation: the update's fixed point is the Oldroyd-B steady state up to a first-order
+    splitting error, which falls tenfold with dt."""
+    wg = Wi * g
+    exact = np.array([2.0 * wg * wg, wg, wg, 0.0])
+    errs = []
+    for dt in (1.0e-3, 1.0e-4):
+        t, trace = logconf_particle([1.0e-2, 1.0e-2, 1.0e-2, 0.0], [0.0, g, 0.0, 0.0], dt, Wi,
+                                    nsteps=int(round(30.0 * Wi / dt)))
+        assert abs(trace - (2.0 + t[0] + t[3])) < 1e-12
+        err = np.abs(t - exact).max() / np.abs(exact).max()
+        assert err < 1.0e-3, (dt, t, exact)
+        errs.append(err)
+    assert 8.0 < errs[0] / errs[1] < 12.0  # first order in dt
+
+
+def test_shear_from_rest_stays_at_rest():
+    """At A = I both eigenvalues are 1 and R = I (calc_eigens, predictor_mod.F90:253-290); the
+    update keeps only the diagonal of R^T grad(u) R in B and puts the shear into the rotation,
+    which acts on log A = 0, so a pure shear leaves the conformation at rest.  Stress starts
+    growing only once the conformation is anisotropic."""
+    t, trace = logconf_particle([0.0, 0.0, 0.0, 0.0], [0.0, 0.5, 0.0, 0.0], 1.0e-3, 1.0, nsteps=5000)
+    assert np.all(t == 0.0) and trace == 2.0
 
 
 def test_bicgstab_solution_satisfies_system():
