@@ -7,8 +7,9 @@
 * at rest the log-conformation step equals the analytic relaxation tau*exp(-dt/Wi) (predictor_mod.F90:318-331);
 * the BiCGSTAB solution satisfies the assembled system;
 * in steady simple shear the log-conformation update converges to the Oldroyd-B relations of
-  docs/docs.tex:93-100 (A_xy = Wi g, tau_xx = 2 (Wi g)^2, tau_yy = 0) at first order in dt, and
-  from rest it stays at rest (the reference's degenerate-eigenvalue branch);
+  docs/docs.tex:93-100 (A_xy = Wi g, tau_xx = 2 (Wi g)^2, tau_yy = 0) and to the closed form of
+  the linear PTT law stated there, at first order in dt, and from rest it stays at rest (the
+  reference's degenerate-eigenvalue branch);
 * the oracle is deterministic for any OpenMP thread count;
 * a regression summary of one step on the shipped Rayleigh-Benard deck.
 """
@@ -115,16 +116,30 @@ def _ell_matvec(o, x, n):
     return o.get("ppe_diag") * x + (np.where(mask, val, 0.0) * x[col]).sum(0)
 
 
-@pytest.mark.parametrize("Wi,g", [(1.0, 0.5), (0.5, 2.0), (2.0, 0.3)])
-def test_steady_shear_matches_oldroyd_b(Wi, g):
-    """Simple shear du/dy = g held for 30 relaxation times from a slightly anisotropic
-    conformation: the update's fixed point is the Oldroyd-B steady state up to a first-order
-    splitting error, which falls tenfold with dt."""
+def steady_shear(Wi, g, eps):
+    """Steady simple shear du/dy = g of the linear PTT law of docs/docs.tex (f_R = [1 + eps
+    tr(A - I)] (A - I), relaxation rate 1/Wi): with Y = 1 + eps tau_xx, tau_yy = 0,
+    tau_xy = Wi g / Y and tau_xx = 2 (Wi g)^2 / Y^2, a cubic in tau_xx solved by Newton.
+    eps = 0 is Oldroyd-B: tau_xy = Wi g, tau_xx = 2 (Wi g)^2."""
     wg = Wi * g
-    exact = np.array([2.0 * wg * wg, wg, wg, 0.0])
+    x = 2.0 * wg * wg
+    for _ in range(100):
+        f = x * (1.0 + eps * x) ** 2 - 2.0 * wg * wg
+        x -= f / ((1.0 + eps * x) ** 2 + 2.0 * eps * x * (1.0 + eps * x))
+    y = 1.0 + eps * x
+    return np.array([x, wg / y, wg / y, 0.0])
+
+
+@pytest.mark.parametrize("Wi,g,eps", [(1.0, 0.5, 0.0), (0.5, 2.0, 0.0), (2.0, 0.3, 0.0),
+                                      (1.0, 1.0, 0.25), (0.5, 2.0, 0.1), (2.0, 0.5, 0.5)])
+def test_steady_shear_matches_the_closed_form(Wi, g, eps):
+    """Simple shear held for 30 relaxation times from a slightly anisotropic conformation: the
+    update's fixed point is the steady state of the Oldroyd-B (eps = 0) or linear PTT law up to
+    a first-order splitting error, which falls tenfold with dt."""
+    exact = steady_shear(Wi, g, eps)
     errs = []
     for dt in (1.0e-3, 1.0e-4):
-        t, trace = logconf_particle([1.0e-2, 1.0e-2, 1.0e-2, 0.0], [0.0, g, 0.0, 0.0], dt, Wi,
+        t, trace = logconf_particle([1.0e-2, 1.0e-2, 1.0e-2, 0.0], [0.0, g, 0.0, 0.0], dt, Wi, eps_ptt=eps,
                                     nsteps=int(round(30.0 * Wi / dt)))
         assert abs(trace - (2.0 + t[0] + t[3])) < 1e-12
         err = np.abs(t - exact).max() / np.abs(exact).max()
