@@ -3,6 +3,7 @@
 * the quintic spline integrates to 1 (ad_7 = 7/(478 pi h^2), input.F90:168);
 * Shepard sum: sum_j W_ij dv + W(0) dv ~ 1 on a lattice (freesurf_mod.F90:95-100);
 * the Bonet-Lok correction makes the gradient of a linear field exact (kernel_calculation.F90:55-66);
+* the Morris pair weight gives the Laplacian of a quadratic field (4 for x^2 + y^2, on average);
 * calc_eigens reconstructs A = R diag(L) R^T (predictor_mod.F90:253-290);
 * at rest the log-conformation step equals the analytic relaxation tau*exp(-dt/Wi) (predictor_mod.F90:318-331);
 * the BiCGSTAB solution satisfies the assembled system;
@@ -128,6 +129,28 @@ def steady_shear(Wi, g, eps):
         x -= f / ((1.0 + eps * x) ** 2 + 2.0 * eps * x * (1.0 + eps * x))
     y = 1.0 + eps * x
     return np.array([x, wg / y, wg / y, 0.0])
+
+
+def test_morris_laplacian_of_a_quadratic():
+    """The viscous and heat-diffusion pair weight w_L = 2 r.gradW / (r^2 + 0.01 h^2)
+    (kernel_calculation.F90:55-66) makes sum_j (f_i - f_j) w_L the Laplacian: for f = x^2 + y^2
+    it averages 4 over the interior of a jittered lattice (pointwise within the operator's
+    scatter on disordered particles), which pins its sign and normalisation."""
+    c = cases.poiseuille(40, seed=2, const_mod=1)
+    c.body_force = (0.0, 0.0)
+    o = OracleSolver(c)
+    o.step()
+    n = c.npfb
+    x, y = o.get("rsx"), o.get("rsy")
+    cnt, link, wl = o.get("ij_count"), o.get("ij_link"), o.get("w_L")
+    kmax = len(link) // n
+    link, wl = link.reshape(kmax, n), wl.reshape(kmax, n)
+    f = x * x + y * y
+    slot = np.arange(kmax)[:, None] < cnt[None, :]
+    lap = np.sum(np.where(slot, (f[:n][None, :] - f[link]) * wl, 0.0), axis=0)
+    inner = (np.arange(n) >= c.nbS) & (x[:n] > 0.2) & (x[:n] < 0.8) & (y[:n] > 0.2) & (y[:n] < 0.8)
+    assert abs(lap[inner].mean() - 4.0) < 0.06, lap[inner].mean()
+    assert np.all(np.abs(lap[inner] - 4.0) < 1.0)
 
 
 @pytest.mark.parametrize("Wi,g,eps", [(1.0, 0.5, 0.0), (0.5, 2.0, 0.0), (2.0, 0.3, 0.0),
