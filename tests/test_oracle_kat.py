@@ -7,6 +7,7 @@
 * calc_eigens reconstructs A = R diag(L) R^T (predictor_mod.F90:253-290);
 * at rest the log-conformation step equals the analytic relaxation tau*exp(-dt/Wi) (predictor_mod.F90:318-331);
 * the BiCGSTAB solution satisfies the assembled system;
+* one step's projection balances a buoyancy that is a pure gradient with the hydrostatic pressure;
 * in steady simple shear the log-conformation update converges to the Oldroyd-B relations of
   docs/docs.tex:93-100 (A_xy = Wi g, tau_xx = 2 (Wi g)^2, tau_yy = 0) and to the closed form of
   the linear PTT law stated there, at first order in dt, and from rest it stays at rest (the
@@ -129,6 +130,40 @@ def steady_shear(Wi, g, eps):
         x -= f / ((1.0 + eps * x) ** 2 + 2.0 * eps * x * (1.0 + eps * x))
     y = 1.0 + eps * x
     return np.array([x, wg / y, wg / y, 0.0])
+
+
+def hydrostatic_step(n):
+    """One step from rest of the periodic channel with buoyancy theta = sin(pi y) and no body
+    force: the pressure's error against the hydrostatic -cos(pi y)/pi (relative to its amplitude)
+    and the largest velocity left, relative to the dt theta the predictor adds."""
+    c = cases.poiseuille(n, seed=2, const_mod=1)
+    c.body_force = (0.0, 0.0)
+    c.u = np.zeros_like(c.u)
+    c.theta = np.sin(np.pi * c.r[:, 1])
+    c.b_thermal = np.zeros(4)
+    c.tol = 1.0e-10
+    o = OracleSolver(c)
+    dt = o.step()["dt"]
+    npfb = c.npfb
+    y, p = o.get("rsy")[:npfb], o.get("p")[:npfb]
+    fl = np.arange(npfb) >= c.nbS
+    pa = -np.cos(np.pi * y) / np.pi
+    err = np.abs((p - p[fl].mean()) - (pa - pa[fl].mean()))[fl].max() / (1.0 / np.pi)
+    vmax = max(np.abs(o.get("ux")[:npfb][fl]).max(), np.abs(o.get("uy")[:npfb][fl]).max())
+    return err, vmax / dt
+
+
+def test_buoyancy_is_balanced_by_the_hydrostatic_pressure():
+    """The projection of one step (ppe_solve_in_house_simple_dirichlet.F90, calc_pressure_gradient):
+    buoyancy theta e_y with theta = sin(pi y) between no-slip walls (theta = 0 there, b_thermal 0,
+    so the wall mirrors' odd reflection continues it exactly) is a pure gradient, balanced by
+    P = -cos(pi y)/pi, whose normal derivative vanishes at the walls as the mirrors impose.  The
+    step's pressure follows it and the velocity the buoyancy adds is removed, both up to the
+    discretisation error, which falls with resolution; a sign or a normalisation error in the
+    right-hand side, the Laplacian or the pressure gradient would leave O(1) of either."""
+    coarse, fine = hydrostatic_step(24), hydrostatic_step(64)
+    assert fine[0] < 0.06 and fine[1] < 0.05, fine
+    assert fine[0] < coarse[0] and fine[1] < coarse[1], (coarse, fine)
 
 
 def test_morris_laplacian_of_a_quadratic():
