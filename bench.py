@@ -668,7 +668,7 @@ def run_reference(args, dist: Dist):
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (same generator and seed as the GPU arm)",
-            "config": {"workload": f"{case.name}: confined cylinder, {case.n_fluid} fluid particles",
+            "config": {"workload": workload_text(args, case),
                        "npfb": case.npfb, "n_fluid": case.n_fluid, "precision": "fp64"},
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads(), "kind": "port", "sample": sample},
