@@ -90,10 +90,12 @@ class ClockSampler:
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index: int):
+    def __init__(self, gpu_index: int, out_dir: str | None = None):
+        import tempfile
         self.gpu = gpu_index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_rank{gpu_index}.csv"
+        d = pathlib.Path(out_dir) if out_dir else pathlib.Path(tempfile.mkdtemp(prefix="vebi_bench_"))
+        self.path = d / f"clocks_rank{gpu_index}.csv"
 
     def __enter__(self):
         try:
@@ -154,15 +156,27 @@ def ppe_bytes_per_iteration(n_rows: int, nnz_off: int, mixed: bool = False) -> f
     return 2.0 * (12.0 * nnz_off + 44.0 * n_rows) + 168.0 * n_rows
 
 
-def workload_text(args, case) -> str:
+def workload_text(args, case, precision: str) -> str:
     Re = (case.Ra / case.Pr) ** 0.5
     common = (f"{case.n_fluid} fluid + {case.nbS} wall particles, dx={case.dx:.4g}, Oldroyd-B Re={Re:.3g} "
-              f"Wi={case.El * Re:.3g} beta={case.beta}, {args.precision}, PPE preconditioner {args.precond}")
+              f"Wi={case.El * Re:.3g} beta={case.beta}, {precision}, PPE preconditioner {args.precond}")
     if args.case == "cylinder_4m":
         return f"{case.name}: confined cylinder, channel 30R x 4R, blockage 0.5, periodic x, " + common
     if args.case.startswith("poiseuille"):
         return f"{case.name}: planar Poiseuille channel 1x1, periodic x, walls y=0,1, body force, " + common
     return f"{case.name}: " + common
+
+
+DATA_TEXT = ("synthetic: seeded jittered lattice (U(-0.01dx,0.01dx)), walls/circle by the reference's "
+             "make_boundary_particles rules; no dataset")
+
+
+def bench_config(args, case, precision: str) -> dict:
+    """The workload description both arms print (the same keys and values on both)."""
+    return {"workload": workload_text(args, case, precision), "npfb": case.npfb, "n_fluid": case.n_fluid,
+            "precision": precision,
+            "l2": (f"inputs larger than L2: the pair arrays and the PPE matrix hold {case.npfb * 75 * 40 / 1e9:.2f} GB "
+                   "(ELL width 75; link 4 B, three weights 24 B, matrix 12 B per slot), no flush")}
 
 
 def stage_bandwidth(stage_ms_per_step: dict, n: int, kbar: float, mixed: bool, peak: float) -> dict:
@@ -248,7 +262,7 @@ def run_gb300(args, dist: Dist):
     for _ in range(args.warmup):
         sol.step()
     dist.barrier()
-    with ClockSampler(dist.local) as clk:
+    with ClockSampler(dist.local, args.out_dir) as clk:
         ms, st = sol.run_steps(args.steps)
     dist.barrier()
     # state after warm-up + timed steps (before the e2e steps), for the precision comparison
@@ -297,48 +311,58 @@ def run_gb300(args, dist: Dist):
             "peak_kind": f"{peak_kind} hbm_gbs (burst copy)",
             "bytes_per_iteration": bytes_iter, "iterations_per_launch": iters_per_step,
             "launch_ms": round(per_launch_s * 1e3, 3)}
-    # end to end through the C-ABI with host buffers (pinned), copies inside the timed region
+    # end to end through the C-ABI with host buffers (pinned), copies inside the timed region:
+    # the time loop of a host driver that owns the state in its arrays (the Fortran module
+    # arrays behind div_free).  Every step uploads the arrays, steps, and downloads the new
+    # state into the same arrays, so the state carries from step to step.
     e2e = None
     if not args.no_e2e:
-        f = case.fortran_planes()
-        host = {k: np.ascontiguousarray(v) for k, v in f.items() if k != "ld"}
-        out = {k: np.zeros_like(host[k]) for k in ("r", "u", "tau", "theta")}
-        out["p"] = np.zeros(case.npfb)
+        n = case.npfb
+        host = sol.download()  # the state the GPU holds after the timed steps
+        host = {k: np.ascontiguousarray(host[k]) for k in ("r", "u", "tau", "theta", "trace_conf", "inbin", "p")}
         pinned = []
-        for a in list(host.values()) + list(out.values()):
+        for a in host.values():
             if sol.lib.vebi_pin_host(a.ctypes.data_as(C.c_void_p), a.nbytes) == 0:
                 pinned.append(a)
         dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
-        # start from the state the GPU holds now (as a driver that owns the host arrays would)
-        sol.download()
         h2d = sum(host[k].nbytes for k in ("r", "u", "tau", "theta", "trace_conf", "inbin"))
-        d2h = sum(out[k].nbytes for k in ("r", "u", "tau", "theta", "p"))
+        d2h = sum(host[k].nbytes for k in ("r", "u", "tau", "theta", "trace_conf", "inbin", "p"))
+        t_up = t_step = t_down = 0.0
         dist.barrier()
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
-            sol.upload(host["r"], host["u"], host["tau"], host["theta"], host["trace_conf"], host["inbin"],
-                       f["ld"])
+            ta = time.perf_counter()
+            sol.upload(host["r"], host["u"], host["tau"], host["theta"], host["trace_conf"], host["inbin"], n)
+            tb = time.perf_counter()
             sol.step()
-            sol.lib.vebi_download_state(sol.h, dp(out["r"]), dp(out["u"]), dp(out["tau"]), dp(out["theta"]),
-                                        dp(out["p"]), None, None, None, None, None, f["ld"])
+            tc = time.perf_counter()
+            sol.lib.vebi_download_state(sol.h, dp(host["r"]), dp(host["u"]), dp(host["tau"]), dp(host["theta"]),
+                                        dp(host["p"]), None, None, dp(host["trace_conf"]), None,
+                                        host["inbin"].ctypes.data_as(C.POINTER(C.c_uint8)), n)
+            td = time.perf_counter()
+            t_up, t_step, t_down = t_up + tb - ta, t_step + tc - tb, t_down + td - tc
         e2e_s = time.perf_counter() - t0
         dist.barrier()
         e2e_s = dist.max(e2e_s)
+        pinned_ok = len(pinned) == len(host)
         for a in pinned:
             sol.lib.vebi_unpin_host(a.ctypes.data_as(C.c_void_p))
+        k = max(args.e2e_steps, 1)
         e2e = {"value": dist.sum(float(n_fluid * args.e2e_steps)) / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
-               "path": "vebi_upload_state + vebi_step + vebi_download_state (pinned host arrays)"}
+               "host_pinned": pinned_ok,
+               "ms_per_step": {"upload_call": round(1e3 * t_up / k, 3), "step": round(1e3 * t_step / k, 3),
+                               "download": round(1e3 * t_down / k, 3)},
+               "path": "vebi_upload_state + vebi_step + vebi_download_state on pinned host arrays that carry "
+                       "the state from step to step (upload is asynchronous; its copies complete inside the step "
+                       "call, whose stats read-back waits for the stream)"}
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == abi.PREC_FP64 else "f32+f64",
-        "data": "synthetic: seeded jittered lattice (U(-0.01dx,0.01dx)), walls/circle by the reference's "
-                "make_boundary_particles rules; no dataset",
-        "config": {"workload": workload_text(args, case),
-                   "npfb": case.npfb, "n_fluid": n_fluid, "precision": args.precision,
-                   "parallelism": f"replicas x{dist.world}",
-                   "l2": "inputs larger than L2 (ELL matrix and pair arrays are several GB)"},
+        "data": DATA_TEXT,
+        "config": bench_config(args, case, args.precision),
+        "parallelism": f"replicas x{dist.world} (the step does not shard; one independent replica per GPU)",
         "LS_iters_per_step": iters_per_step,
         "LS_residual_last": st["LS_residual"],
         "stage_ms_per_step": {abi.STAGE_NAMES[i]: round(v / args.steps, 3) for i, v in enumerate(stage) if v > 0},
@@ -358,7 +382,7 @@ def run_gb300(args, dist: Dist):
     return res
 
 
-def run_adjoint(args, dist: Dist) -> dict:
+def run_adjoint(args, dist: Dist, ref: dict | None = None) -> dict:
     """Reverse mode on the heated-cavity workload (differentially heated square cavity,
     args.adjoint_side^2 fluid particles, Ra=1e5, Pr=1, Oldroyd-B Wi=0.5, beta=0.5, seeded
     perturbed temperature), FP64 or mixed-precision step (args.adjoint_precision) with the
@@ -366,8 +390,10 @@ def run_adjoint(args, dist: Dist) -> dict:
     after a window of args.adjoint steps, dJ/dtheta0 (full field) and dJ/dWi, checkpoints every
     args.checkpoint steps.  Forward cost = the plain steps of the window (captured graph);
     adjoint cost = the reverse sweep, its recompute of every segment included.  With
-    args.adjoint_fd > 0, that many seeded directions are checked by central differences of the
-    replayed window."""
+    args.adjoint_fd > 0, that many seeded directions of theta0, and Wi, are checked by central
+    differences of the replayed window (step args.adjoint_eps).  `ref` is the result of another
+    run on the same workload (the FP64 window): the directional derivatives along the same
+    seeded directions and dJ/dWi are reported against it."""
     from vebisph_gb300 import abi, cases
     from vebisph_gb300.solver import Adjoint, StepSolver
     if dist.rank != 0:
@@ -400,22 +426,55 @@ def run_adjoint(args, dist: Dist) -> dict:
     t0 = time.perf_counter()
     g = adj.reverse(seed_u=seed)
     t_rev = time.perf_counter() - t0
-    fd = []
-    for k in range(args.adjoint_fd):
+    def kinetic():
+        u = s.download()["u"]
+        return 0.5 * float(np.mean(u[0, nbS:] ** 2 + u[1, nbS:] ** 2))
+
+    def direction(k):
         rng = np.random.default_rng(1000 + k)
         d = np.zeros(n)
         d[nbS:] = rng.normal(size=n - nbS)
-        d /= np.abs(d).max()
-        eps = 1.0e-3
+        return d / np.abs(d).max()
+
+    # central differences of the replayed window (the differentiated map) along seeded
+    # unit-max directions of theta0, step args.adjoint_eps; and of Wi, step eps * Wi
+    eps = args.adjoint_eps
+    fd = []
+    t0 = time.perf_counter()
+    for k in range(args.adjoint_fd):
+        d = direction(k)
         js = []
         for sgn in (1.0, -1.0):
             s.upload(st0["r"], st0["u"], st0["tau"], st0["theta"] + sgn * eps * d, st0["trace_conf"], st0["inbin"], n)
             adj.replay(N)
-            u = s.download()["u"]
-            js.append(0.5 * float(np.mean(u[0, nbS:] ** 2 + u[1, nbS:] ** 2)))
+            js.append(kinetic())
         f = (js[0] - js[1]) / (2 * eps)
         a = float(g["theta"] @ d)
-        fd.append({"fd": f, "adjoint": a, "rel_err": abs(f - a) / max(abs(f), 1e-300)})
+        fd.append({"direction": k, "fd": f, "adjoint": a, "rel_err": abs(f - a) / max(abs(f), 1e-300)})
+    fd_wi = None
+    if args.adjoint_fd and case.const_mod != 1:
+        wi0 = 0.5
+        h = eps * wi0
+        js = []
+        for sgn in (1.0, -1.0):
+            s.set_weissenberg(wi0 + sgn * h)
+            s.upload(st0["r"], st0["u"], st0["tau"], st0["theta"], st0["trace_conf"], st0["inbin"], n)
+            adj.replay(N)
+            js.append(kinetic())
+        s.set_weissenberg(wi0)
+        f = (js[0] - js[1]) / (2 * h)
+        fd_wi = {"fd": f, "adjoint": g["wi"], "rel_err": abs(f - g["wi"]) / max(abs(f), 1e-300)}
+    t_fd = time.perf_counter() - t0
+    # directional derivatives along the same seeded directions, for a run compared with this one
+    dirs = [float(g["theta"] @ direction(k)) for k in range(args.adjoint_dirs)]
+    vs = None
+    if ref is not None:
+        rd = ref["directional_derivatives"]
+        vs = {"directional_rel_diff": [abs(x - y) / max(abs(y), 1e-300) for x, y in zip(dirs, rd)],
+              "dJ_dWi_rel_diff": abs(g["wi"] - ref["dJ_dWi"]) / max(abs(ref["dJ_dWi"]), 1e-300)}
+        if ref.get("finite_differences"):
+            vs["vs_fp64_fd_rel"] = [abs(x - e["fd"]) / max(abs(e["fd"]), 1e-300)
+                                    for x, e in zip(dirs, ref["finite_differences"])]
     adj.close()
     s.close()
     solver = ("the multigrid-preconditioned PPE (forward and transposed)" if args.precond == "multigrid"
@@ -432,7 +491,14 @@ def run_adjoint(args, dist: Dist) -> dict:
             "reverse_ms_per_step": 1e3 * t_rev / N, "adjoint_over_forward": t_rev / t_fwd,
             "forward_LS_iters_per_step": fwd_iters / N, "transposed_LS_iters_per_step": g["ls_iters"] / N,
             "dJ_dWi": g["wi"], "grad_theta_max_abs": float(np.abs(g["theta"]).max()),
+            "directional_derivatives": dirs,
             "finite_differences": fd,
+            "fd_eps": eps if fd else None,
+            "fd_within_1e-5": (f"{sum(e['rel_err'] <= 1e-5 for e in fd)}/{len(fd)}" if fd else None),
+            "fd_rel_err_max": max((e["rel_err"] for e in fd), default=None),
+            "fd_dJ_dWi": fd_wi,
+            "fd_seconds": round(t_fd, 1),
+            "vs_fp64_window": vs,
             "timing": "host wall clock around the synchronous calls (each call waits for its GPU work)"}
 
 
@@ -459,7 +525,7 @@ def run_batch(args, dist: Dist):
     for _ in range(args.warmup):
         b.step(1)
     dist.barrier()
-    with ClockSampler(dist.local) as clk:
+    with ClockSampler(dist.local, args.out_dir) as clk:
         ms, stats = b.step(args.steps)
     dist.barrier()
     done += args.warmup + args.steps
@@ -532,11 +598,9 @@ def run_batch(args, dist: Dist):
                          f"{args.steps} steps from the initial state"}
     du, dp, spread = np.array(du), np.array(dp), np.array(spread)
     counts = np.array([c.n_fluid for c in cl])
-    try:
-        (ROOT / "gpurun_out").mkdir(exist_ok=True)
-        (ROOT / "gpurun_out" / f"batch{args.batch}_instances.json").write_text(json.dumps(per))
-    except OSError:
-        pass
+    if args.out_dir:  # the per-instance records
+        pathlib.Path(args.out_dir).mkdir(parents=True, exist_ok=True)
+        (pathlib.Path(args.out_dir) / f"batch{args.batch}_instances.json").write_text(json.dumps(per))
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
@@ -577,16 +641,10 @@ def run_batch(args, dist: Dist):
 
 
 def drag_summary(case, st: dict, fields: dict):
-    """Force of the fluid on the cylinder after the last timed step (the circle-mirror pair
-    terms of the step) and the drag coefficient K = F_x / (eta0 U): eta0 = sqrt(Pr/Ra) the total
-    viscosity 1/Re, U the mean fluid x-velocity."""
-    if not case.nb_circles:
-        return None
-    fx, fy = st["circle_force"]
-    fl = slice(case.nbS, case.npfb)
-    u_mean = float(np.mean(fields["ux"][fl]))
-    eta0 = (case.Pr / case.Ra) ** 0.5
-    return {"F_x": fx, "F_y": fy, "U_mean": u_mean, "K": fx / (eta0 * u_mean)}
+    """Force of the fluid on the cylinder after the last timed step and the drag coefficient
+    (vebisph_gb300/diagnostics.py)."""
+    from vebisph_gb300 import diagnostics
+    return diagnostics.drag(case, st["circle_force"], fields["ux"])
 
 
 def mixed_summary(f64: dict, mx: dict) -> dict:
@@ -597,11 +655,9 @@ def mixed_summary(f64: dict, mx: dict) -> dict:
     us = max(np.abs(b["ux"]).max(), np.abs(b["uy"]).max())
     du = max(np.abs(a["ux"] - b["ux"]).max(), np.abs(a["uy"] - b["uy"]).max()) / us
     dp = np.abs(a["p"] - b["p"]).max() / max(np.abs(b["p"]).max(), 1e-300)
-    wake = b["rx"] > 1.0  # behind the cylinder (centred at x = 0); the whole channel elsewhere
-    if not wake.any():
-        wake = np.ones_like(wake)
-    n1a = float((a["tau11"] - a["tau22"])[wake].max())
-    n1b = float((b["tau11"] - b["tau22"])[wake].max())
+    from vebisph_gb300 import diagnostics
+    n1a = diagnostics.n1_wake_max(b["rx"], a["tau11"], a["tau22"])
+    n1b = diagnostics.n1_wake_max(b["rx"], b["tau11"], b["tau22"])
     dt11 = np.abs(a["tau11"] - b["tau11"]).max() / max(np.abs(b["tau11"]).max(), 1e-300)
     return {"value": mx["value"], "unit": UNIT, "ms_per_step": mx["ms_per_step"],
             "speedup_vs_fp64": mx["value"] / f64["value"], "LS_iters_per_step": mx["LS_iters_per_step"],
@@ -641,7 +697,15 @@ def multigrid_summary(plain: dict, f64: dict, mx: dict, pert: dict | None = None
 
 def run_reference(args, dist: Dist):
     """The reference's own CPU path timed on this host: the oracle restatement (the Fortran
-    reference has no compiler here), all host threads, each step a bounded sample."""
+    reference has no compiler here), all host threads.
+
+    A full step of the 4M workload takes ~30 s on 16 cores (its BiCGSTAB runs to the
+    1000-iteration cap), so the K timed steps are bounded samples: each is a whole step with
+    BiCGSTAB capped at args.cpu_iters iterations, and `ms_per_step` is their measured mean.
+    `value` is measured too: one full step at the workload's own cap, run once after the
+    warm-up (`full_step`), converted to particle-steps/s.  The samples' model -- non-solver
+    time + per-iteration time x the full step's iterations -- is reported beside it with its
+    error against that full step."""
     if dist.rank != 0:
         return None
     from oracle.oracle import OracleSolver, threads
@@ -650,27 +714,48 @@ def run_reference(args, dist: Dist):
     o.set_itermax(args.cpu_iters)
     for _ in range(args.warmup):
         o.step()
-    tot = 0.0
-    solve = 0.0
+    full = None
+    if not args.no_full_step:
+        o.set_itermax(case.itermax)
+        t0 = time.perf_counter()
+        s = o.step()
+        full = {"wall_ms": 1e3 * (time.perf_counter() - t0), "LS_iters": s["LS_iters"],
+                "LS_residual": s["LS_residual"], "stage_total_ms": s["stage_ms"][14]}
+        o.set_itermax(args.cpu_iters)
+    tot = solve = wall = 0.0
     iters = 0
     for _ in range(args.steps):
+        t0 = time.perf_counter()
         s = o.step()
+        wall += time.perf_counter() - t0
         tot += s["stage_ms"][14]
         solve += s["stage_ms"][10]
         iters += s["LS_iters"]
+    o.close()
     per_iter = solve / max(iters, 1)
     rest = (tot - solve) / args.steps
-    t_step = rest + per_iter * args.ref_iters
-    value = case.n_fluid / (t_step * 1e-3)
-    sample = (f"{args.steps} oracle steps, BiCGSTAB capped at {args.cpu_iters} iterations; "
-              f"non-solver {rest:.0f} ms/step + {per_iter:.1f} ms/iteration scaled to {args.ref_iters} "
-              f"iterations/step")
+    sample_ms = 1e3 * wall / args.steps
+    model_iters = full["LS_iters"] if full else args.ref_iters
+    model_ms = rest + per_iter * model_iters
+    if full:
+        value = case.n_fluid / (full["wall_ms"] * 1e-3)
+        basis = (f"one full step measured after the warm-up: {full['wall_ms']:.0f} ms, "
+                 f"{full['LS_iters']} BiCGSTAB iterations (the workload's cap {case.itermax})")
+    else:
+        value = case.n_fluid / (model_ms * 1e-3)
+        basis = f"modelled from the samples at {model_iters:.0f} iterations/step (no full step run)"
+    sample = (f"{args.steps} timed oracle steps of the same state, each a whole step with BiCGSTAB capped at "
+              f"{args.cpu_iters} iterations: {sample_ms:.0f} ms/step measured (non-solver {rest:.0f} ms + "
+              f"{per_iter:.1f} ms/iteration); value: {basis}")
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (same generator and seed as the GPU arm)",
-            "config": {"workload": workload_text(args, case),
-                       "npfb": case.npfb, "n_fluid": case.n_fluid, "precision": "fp64"},
+            "warmup": args.warmup, "ms_per_step": sample_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": DATA_TEXT,
+            "config": bench_config(args, case, "fp64"),
             "impl": "reference",
+            "value_measured": full is not None,
+            "full_step": full,
+            "sampled_step_model": {"ms_per_full_step": model_ms, "iterations": model_iters,
+                                   "error_vs_full_step": (model_ms / full["wall_ms"] - 1.0) if full else None},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads(), "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -688,12 +773,17 @@ def main():
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--precond", choices=["none", "multigrid"], default="none",
                     help="opt-in PPE preconditioner (none = the reference's solver)")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=0,
+                    help="steps of the end-to-end loop (default: the same as --steps)")
     ap.add_argument("--cpu-iters", type=int, default=20, help="BiCGSTAB cap of the CPU sample")
     ap.add_argument("--ref-iters", type=float, default=1001.0,
                     help="iterations/step the reference-arm sample is scaled to")
     ap.add_argument("--itermax", type=int, default=0, help="override the PPE iteration cap (profiling runs)")
+    ap.add_argument("--out-dir", default=None,
+                    help="folder for the clock samples and the batch's per-instance records (default: a temp folder)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-full-step", action="store_true",
+                    help="reference arm: skip the one full step that its value is measured on")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision comparison run")
     ap.add_argument("--no-multigrid", action="store_true", help="skip the multigrid-preconditioned runs")
@@ -709,9 +799,14 @@ def main():
     ap.add_argument("--adjoint-side", type=int, default=1024, help="cavity lattice side of the adjoint run")
     ap.add_argument("--checkpoint", type=int, default=20, help="adjoint checkpoint interval")
     ap.add_argument("--adjoint-fd", type=int, default=0, help="finite-difference directions checked at scale")
+    ap.add_argument("--adjoint-eps", type=float, default=1.0e-6, help="central-difference step (unit-max directions)")
+    ap.add_argument("--adjoint-dirs", type=int, default=8,
+                    help="seeded directions whose directional derivatives are reported (and compared across runs)")
     ap.add_argument("--adjoint-tol", type=float, default=1.0e-8, help="PPE tolerance of the adjoint workload")
     ap.add_argument("--adjoint-spinup", type=int, default=20, help="steps run before the adjoint window")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement of the default line")
+    ap.add_argument("--default-adjoint-fd", type=int, default=4,
+                    help="central-difference directions of the default line's adjoint (each replays the window twice)")
     ap.add_argument("--adjoint-precision", default="fp64", choices=["fp64", "mixed"],
                     help="arithmetic of the adjoint workload's forward step")
     ap.add_argument("--adjoint-const-mod", type=int, default=2, choices=[1, 2],
@@ -719,6 +814,8 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.e2e_steps <= 0:
+        args.e2e_steps = args.steps
     if args.batch:
         # independent instances run as concurrent graph branches: more hardware queues
         os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
@@ -761,14 +858,17 @@ def main():
             res["multigrid"] = multigrid_summary(res, runs[0], runs[1], runs[2])
         if not args.no_adjoint and not args.batch and dist.rank == 0:
             # the metric's second part: adjoint/forward cost on the heated cavity (1M)
+            # the configured window: 200 steps, checkpoints every 20, multigrid PPE; FP64 with
+            # central differences (FP64, step 1e-6) along seeded directions and of Wi, then the
+            # configuration's mixed-precision step against it
             aargs = argparse.Namespace(**vars(args))
-            aargs.adjoint, aargs.checkpoint, aargs.precond = 20, 5, "multigrid"
-            aargs.adjoint_tol, aargs.adjoint_fd, aargs.adjoint_const_mod = 1.0e-8, 0, 2
+            aargs.adjoint, aargs.checkpoint, aargs.precond = 200, 20, "multigrid"
+            aargs.adjoint_tol, aargs.adjoint_fd, aargs.adjoint_const_mod = 1.0e-8, args.default_adjoint_fd, 2
             aargs.adjoint_precision = "fp64"
+            aargs.adjoint_dirs = max(args.default_adjoint_fd, 1)
             res["adjoint"] = run_adjoint(aargs, dist)
-            # the same window with the mixed-precision forward step (the configuration's FP32 step)
-            aargs.adjoint_precision = "mixed"
-            res["adjoint_mixed"] = run_adjoint(aargs, dist)
+            aargs.adjoint_precision, aargs.adjoint_fd = "mixed", 0
+            res["adjoint_mixed"] = run_adjoint(aargs, dist, ref=res["adjoint"])
         res.pop("_fields", None)
     else:
         from oracle import build as ob

@@ -47,7 +47,9 @@ enum {
   VEBI_ERR_MIRROR_CAPACITY = 7,/* new: the reference overruns irelation(npfb+1:npfb+esti)     */
   VEBI_ERR_TIMEOUT = 8,        /* a bounded device-side wait gave up                          */
   VEBI_ERR_NO_DEVICE = 9,      /* no usable CUDA device                                       */
-  VEBI_ERR_BOUNDARY = 10       /* check_boundaries failed (input.F90:190-244)                 */
+  VEBI_ERR_BOUNDARY = 10,      /* check_boundaries failed (input.F90:190-244)                 */
+  VEBI_ERR_DIVERGED = 11       /* new, opt-in (vebi_set_velocity_limit): a particle velocity
+                                  became non-finite or exceeded the limit                      */
 };
 
 /* warning bits in vebi_step_stats.warnings (the reference prints and continues) */
@@ -196,6 +198,14 @@ int vebi_set_timing(vebi_ctx* ctx, int32_t on);
 int vebi_debug_size(vebi_ctx* ctx, const char* name, int64_t* elem_bytes, int64_t* count);
 int vebi_debug_get(vebi_ctx* ctx, const char* name, void* out, int64_t bytes);
 
+/* Failure-detection check (no reference counterpart; the reference has no device waits):
+ * runs the solvers' bounded grid barrier in a cooperative grid of `blocks` (2..64) blocks in
+ * which one block never arrives, with a short poll limit (1..2^22 polls, about 64 ns each).
+ * The waiting blocks give up, record VEBI_ERR_TIMEOUT and return; *status_out receives the
+ * recorded status and *ms_out (optional) the kernel's duration.  Nothing hangs, and the
+ * CUDA context stays usable. */
+int vebi_test_barrier_timeout(int32_t blocks, int64_t spin_limit, int32_t* status_out, double* ms_out);
+
 /* ---- A PPE solve that allocates nothing.  No counterpart in the reference. ------------
  * For callers that cannot call cudaMalloc -- a host framework whose allocator owns all device
  * memory, or a real-time loop that must not allocate -- this runs the step's BiCGSTAB
@@ -209,7 +219,11 @@ int vebi_debug_get(vebi_ctx* ctx, const char* name, void* out, int64_t bytes);
  *  - the first call on a device looks up the array's device address with that device
  *    current; make that first call before any stream capture begins.
  * `stream` is a cudaStream_t (NULL = legacy default stream).  When iters_out or residual_out
- * is non-NULL the call waits for the solve and reports them. */
+ * is non-NULL the call waits for the solve, reports them and returns the solve's device-side
+ * status (VEBI_ERR_TIMEOUT when a grid barrier gave up); those pointers must be NULL while the
+ * stream is being captured (VEBI_ERR_ARG otherwise).  With both NULL the call only enqueues
+ * the solve and returns launch errors: a device-side failure then shows in x, which the
+ * kernel fills with NaN. */
 #define VEBI_NOALLOC_MAX_ROWS 65536
 int vebi_ppe_solve_noalloc(const int32_t* ij_count, const int32_t* ppe_col, const double* ppe_val,
                            const double* ppe_diag, const double* rhs, double* x, int32_t n,
@@ -301,6 +315,15 @@ typedef struct vebi_adjoint vebi_adjoint;
  * relaxation time of the log-conformation update and the polymeric coefficient
  * (1-beta)/(Re Wi).  For parameter continuation and for checking dJ/dWi. */
 int vebi_set_weissenberg(vebi_ctx* ctx, double wi);
+
+/* Divergence guard (opt-in; no reference counterpart -- the reference runs on until positions
+ * turn NaN and are binned, put_in_bin.F90:27-47).  With u_limit > 0, a step whose fluid
+ * velocity entering it, or whose new fluid or wall velocity, is non-finite or above u_limit
+ * in magnitude fails with VEBI_ERR_DIVERGED; like every step failure the status is sticky
+ * until the next vebi_upload_state.  In a batch this is each instance's own status
+ * (stats[i].error), so a simulation that blows up cannot pass silently.  u_limit = 0 turns
+ * the guard off (the default). */
+int vebi_set_velocity_limit(vebi_ctx* ctx, double u_limit);
 int vebi_adjoint_create(vebi_ctx* ctx, int32_t max_steps, int32_t checkpoint_every, vebi_adjoint** out);
 int vebi_adjoint_record(vebi_adjoint* adj, int32_t nsteps, vebi_step_stats* last);
 int vebi_adjoint_replay(vebi_adjoint* adj, int32_t nsteps, vebi_step_stats* last);

@@ -9,7 +9,7 @@ list_directed.json: the SHA-256 of the shipped IPART text (gfortran list-directe
   output, datclass.F90:649-651) and sample lines of it and of IBOUND (integer items,
   datclass.F90:686-700): the golden vectors of the library's list-directed formatter.
 
-Usage: python tests/golden/make_fixtures.py [/path/to/reference]
+Usage: python -m tests.golden.make_fixtures <reference checkout>  (the argument is required)
 """
 from __future__ import annotations
 
@@ -61,7 +61,9 @@ def list_directed_summary(gen: pathlib.Path) -> dict:
 
 
 def main():
-    ref = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python -m tests.golden.make_fixtures <reference checkout (the vebisph source tree)>")
+    ref = pathlib.Path(sys.argv[1])
     deck = cases.read_deck(ref / "source" / "gen")
     (HERE / "rb_deck_digest.json").write_text(json.dumps(deck_summary(deck), indent=1) + "\n")
     (HERE / "oracle_rb_step1.json").write_text(json.dumps(oracle_summary(deck), indent=1) + "\n")

@@ -379,3 +379,50 @@ def test_reverse_sweep_is_deterministic():
     assert g1["wi"] == g2["wi"] and g1["ls_iters"] == g2["ls_iters"]
     adj.close()
     s.close()
+
+
+@pytest.fixture(scope="module")
+def long_window():
+    """A 128 x 128 Oldroyd-B heated cavity (16k fluid particles, Ra 1e4, Wi 0.5) over a 50-step
+    window with checkpoints every 10, after 20 steps of spin-up: 64x the particles and 8x the
+    steps of the 16x16 window, with five checkpoint segments to restore and replay."""
+    case = cases.cavity(n=128, seed=5, Ra=1.0e4, Wi=0.5, beta=0.5, amp=2.0e-2)
+    case.tol = 1.0e-11
+    case.itermax = 8000
+    s = StepSolver(case)
+    for _ in range(20):
+        s.step()
+    st0 = s.download()
+    adj = Adjoint(s, max_steps=50, checkpoint_every=10)
+    adj.record(50)
+    fin = s.download()
+    nbS, n = case.nbS, case.npfb
+    seed = np.zeros((2, n))
+    seed[:, nbS:] = fin["u"][:, nbS:] / (n - nbS)
+    g = adj.reverse(seed_u=seed)
+    yield dict(case=case, s=s, adj=adj, st0=st0, g=g)
+    adj.close()
+    s.close()
+
+
+@pytest.mark.parametrize("field", ["theta", "tau"])
+def test_long_window_matches_the_tangent_linear_model(long_window, field):
+    """The GPU adjoint of the 50-step window against the oracle's FP64 tangent-linear model of
+    the same window from the same state: the temperature path and the log-conformation
+    (stress) path.  Both solves stop at a relative residual of 1e-11, which bounds their
+    difference; 1e-6 leaves room for its growth over the 50 steps."""
+    w = long_window
+    case, n, nbS = w["case"], w["case"].npfb, w["case"].nbS
+    d = direction(w, field, 21)
+    t = TangentLinear(case, state=w["st0"])
+    t.set_direction(**{{"tau": "dtau", "theta": "dtheta"}[field]: d})
+    for _ in range(50):
+        t.step()
+    (ux, dux), (uy, duy) = t.get("ux"), t.get("uy")
+    t.close()
+    tl = float(np.sum(ux[nbS:n] * dux[nbS:n] + uy[nbS:n] * duy[nbS:n]) / (n - nbS))
+    ad = float(np.sum(w["g"][field] * d))
+    print(f"128x128 cavity, 50 steps, d/d{field}: adjoint {ad:.12e} tangent-linear {tl:.12e} "
+          f"rel {abs(ad - tl) / abs(tl):.3e}")
+    assert abs(tl) > 0
+    assert abs(ad - tl) <= 1.0e-6 * abs(tl), (ad, tl)

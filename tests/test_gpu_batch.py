@@ -70,3 +70,37 @@ def test_failed_instance_is_reported_and_the_others_go_on(built):
             assert np.array_equal(b.instances[i].get(nm)[: cl[i].npfb], s.get(nm)[: cl[i].npfb]), (i, nm)
         s.close()
     b.close()
+
+
+def test_diverging_instance_is_flagged(built):
+    """The opt-in divergence guard: an instance whose velocity passes its limit (here a limit
+    below the flow's own velocity, standing in for a blow-up) fails with VEBI_ERR_DIVERGED in
+    its own stats, sticky like every step failure; the other instances go on unchanged.  A
+    NaN velocity in an uploaded state fails the same way."""
+    from vebisph_gb300.solver import BatchSolver, StepSolver
+    cl = [cases.poiseuille(24, seed=1), cases.cylinder(6.0e3, Wi=0.3, seed=3), cases.poiseuille(20, seed=4)]
+    b = BatchSolver(cl, precision=abi.PREC_MIXED)
+    for inst in b.instances:
+        inst.set_velocity_limit(1.0e3)
+    b.instances[1].set_velocity_limit(1.0e-3)  # the cylinder starts at ~1
+    ms, stats = b.step(2)
+    assert [st["error"] for st in stats] == [0, abi.STATUS["VEBI_ERR_DIVERGED"], 0]
+    for i in (0, 2):
+        s = StepSolver(cl[i], precision=abi.PREC_MIXED)
+        for _ in range(2):
+            s.step()
+        for nm in ("ux", "uy", "p"):
+            assert np.array_equal(b.instances[i].get(nm)[: cl[i].npfb], s.get(nm)[: cl[i].npfb]), (i, nm)
+        s.close()
+    b.close()
+    c = cases.poiseuille(20, seed=5)
+    c.u[c.nbS + 3] = [np.nan, 0.0]
+    s = StepSolver(c)
+    s.set_velocity_limit(1.0e3)
+    st = s.lib.vebi_step(s.h, s.x_mint, s.y_mint, s.x_maxt, s.y_maxt, 0, None)
+    assert st == abi.STATUS["VEBI_ERR_DIVERGED"], st
+    s.set_velocity_limit(0.0)  # off: the reference's behaviour, the NaN particle goes to the bin
+    f = c.fortran_planes()
+    s.upload(f["r"], f["u"], f["tau"], f["theta"], f["trace_conf"], f["inbin"], f["ld"])
+    assert s.step()["n_inbin"] == 1
+    s.close()

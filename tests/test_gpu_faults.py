@@ -64,3 +64,23 @@ def test_box_mismatch_rejected(Solver):
     sol = S(c)
     with pytest.raises(E):
         sol.div_free(sol.x_mint - 1.0, sol.y_mint, sol.x_maxt, sol.y_maxt)
+
+
+def test_grid_barrier_gives_up_and_context_stays_usable(Solver):
+    """The solvers' bounded grid barrier, made to run out: one block of a cooperative grid
+    never arrives (a wait that nothing ends), the others give up after a short poll limit
+    and record VEBI_ERR_TIMEOUT.  The host reads the status; the same process then creates a
+    fresh context and steps it normally."""
+    import ctypes as C
+    S, _ = Solver
+    lib = abi.load_library()
+    st, ms = C.c_int32(-1), C.c_double(0.0)
+    assert lib.vebi_test_barrier_timeout(8, 1 << 14, C.byref(st), C.byref(ms)) == 0, lib.vebi_last_error()
+    assert st.value == abi.STATUS["VEBI_ERR_TIMEOUT"], st.value
+    assert ms.value < 1000.0, ms.value  # ~1e4 polls of ~64 ns: milliseconds, not the solvers' seconds
+    c = cases.poiseuille(20, seed=0)
+    s = S(c).step()
+    assert s["error"] == 0 and s["LS_iters"] >= 1
+    # arguments outside the bounds are refused before anything runs
+    assert lib.vebi_test_barrier_timeout(1, 1 << 14, C.byref(st), None) == abi.STATUS["VEBI_ERR_ARG"]
+    assert lib.vebi_test_barrier_timeout(8, 1 << 30, C.byref(st), None) == abi.STATUS["VEBI_ERR_ARG"]

@@ -45,6 +45,17 @@ def test_mixed_matches_fp64(built, name):
     if name != "poiseuille40":  # body-force driven: P is ~0 there
         perr = np.abs(mx["p"] - f64["p"]).max() / np.abs(f64["p"]).max()
         assert perr < 1e-4, perr
+    # and against the FP64 oracle over the same 10 steps from the same input
+    from oracle.oracle import OracleSolver
+    ref = OracleSolver(CASES[name]())
+    for _ in range(10):
+        ref.step()
+    n = len(f64["ux"])
+    ou = {k: ref.get(k)[:n] for k in ("ux", "uy")}
+    ref.close()
+    oscale = max(np.abs(ou["ux"]).max(), np.abs(ou["uy"]).max())
+    oerr = max(np.abs(mx["ux"] - ou["ux"]).max(), np.abs(mx["uy"] - ou["uy"]).max()) / oscale
+    assert oerr < 1e-4, oerr
 
 
 def case_h(name):

@@ -1,0 +1,74 @@
+"""Mixed-precision step against FP64 on the ~4M confined cylinder at Wi = 0.3, 0.6 and 0.9.
+
+The configuration's target: drag and the peak first normal-stress difference in the wake
+within 1e-4 relative of FP64.  Two comparisons per Weissenberg number:
+
+* against the FP64 oracle, one step from the same input with both BiCGSTAB solves capped at
+  the same 20 iterations (the oracle cannot run the 4M step's uncapped solve in a test's time);
+* against the FP64 GPU step over 8 steps, both with the multigrid-preconditioned PPE
+  converging to tol 1e-8 every step (the reference's unpreconditioned solve stops at its
+  1000-iteration cap on this workload, so the two precisions would be compared unconverged).
+
+Drag and N1 are defined in vebisph_gb300/diagnostics.py.
+"""
+import numpy as np
+import pytest
+
+from vebisph_gb300 import abi, cases, diagnostics
+
+pytestmark = pytest.mark.gpu
+
+WIS = (0.3, 0.6, 0.9)
+
+
+def _fields(s, n):
+    return {k: s.get(k)[:n].copy() for k in ("rx", "ux", "uy", "tau11", "tau22")}
+
+
+def _n1(f):
+    return diagnostics.n1_wake_max(f["rx"], f["tau11"], f["tau22"])
+
+
+@pytest.mark.parametrize("wi", WIS)
+def test_mixed_vs_fp64_oracle_one_step(built, wi):
+    from oracle.oracle import OracleSolver
+    from vebisph_gb300.solver import StepSolver
+    case = cases.cylinder(4.0e6, Wi=wi, seed=0)
+    case.itermax = 20
+    n = case.npfb
+    mx = StepSolver(case, precision=abi.PREC_MIXED)
+    sm = mx.step()
+    fm = _fields(mx, n)
+    mx.close()
+    ref = OracleSolver(case)
+    so = ref.step()
+    fo = _fields(ref, n)
+    ref.close()
+    drag_rel = diagnostics.rel(sm["circle_force"][0], so["circle_force"][0])
+    n1_rel = diagnostics.rel(_n1(fm), _n1(fo))
+    us = max(np.abs(fo["ux"]).max(), np.abs(fo["uy"]).max())
+    du = max(np.abs(fm["ux"] - fo["ux"]).max(), np.abs(fm["uy"] - fo["uy"]).max()) / us
+    print(f"Wi={wi}: mixed vs FP64 oracle, drag {drag_rel:.3g}, N1 {n1_rel:.3g}, u {du:.3g}")
+    assert drag_rel <= 1e-4 and n1_rel <= 1e-4 and du <= 1e-4, (drag_rel, n1_rel, du)
+
+
+@pytest.mark.parametrize("wi", WIS)
+def test_mixed_vs_fp64_multigrid_eight_steps(built, wi):
+    from vebisph_gb300.solver import StepSolver
+    out = {}
+    for prec in (abi.PREC_FP64, abi.PREC_MIXED):
+        case = cases.cylinder(4.0e6, Wi=wi, seed=0)
+        case.ppe_precond = abi.PRECOND_MULTIGRID
+        s = StepSolver(case, precision=prec)
+        for _ in range(8):
+            st = s.step()
+            assert st["LS_residual"] <= 1e-8, st["LS_residual"]
+        out[prec] = (st, _fields(s, case.npfb))
+        s.close()
+    (s64, f64), (smx, fmx) = out[abi.PREC_FP64], out[abi.PREC_MIXED]
+    drag_rel = diagnostics.rel(smx["circle_force"][0], s64["circle_force"][0])
+    n1_rel = diagnostics.rel(_n1(fmx), _n1(f64))
+    us = max(np.abs(f64["ux"]).max(), np.abs(f64["uy"]).max())
+    du = max(np.abs(fmx["ux"] - f64["ux"]).max(), np.abs(fmx["uy"] - f64["uy"]).max()) / us
+    print(f"Wi={wi}: mixed vs FP64 (multigrid, 8 steps), drag {drag_rel:.3g}, N1 {n1_rel:.3g}, u {du:.3g}")
+    assert drag_rel <= 1e-4 and n1_rel <= 1e-4 and du <= 1e-4, (drag_rel, n1_rel, du)

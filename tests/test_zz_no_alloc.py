@@ -10,6 +10,8 @@ import ctypes as C
 import numpy as np
 import pytest
 
+from vebisph_gb300 import cases
+
 pytestmark = pytest.mark.gpu
 
 
@@ -26,14 +28,23 @@ def _system(case_fn, steps=2):
     return out
 
 
-@pytest.mark.parametrize("which", ["poiseuille40", "rb_deck"])
+SYSTEMS = {
+    # closed domains: SPARSE_PBICGSTAB_nonull (linear_solver.F90:275-425)
+    "poiseuille40": (lambda: cases.poiseuille(40, seed=11), 1),
+    "rb_deck": (cases.rayleigh_benard_deck, 1),
+    # an open domain with free-surface rows: the Jacobi SPARSE_PBICGSTAB (linear_solver.F90:82-227)
+    "free_surface_open": (lambda: cases.free_surface_periodic(75, seed=5), 0),
+}
+
+
+@pytest.mark.parametrize("which", sorted(SYSTEMS))
 def test_noalloc_matches_step_solve_twice(built, which):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device visible to torch")
-    from vebisph_gb300 import abi, cases
+    from vebisph_gb300 import abi
     lib = abi.load_library()
-    fn = {"poiseuille40": lambda: cases.poiseuille(40, seed=11), "rb_deck": cases.rayleigh_benard_deck}[which]
+    fn, closed = SYSTEMS[which]
     sysm = _system(fn)
     n = sysm["n"]
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -45,7 +56,7 @@ def test_noalloc_matches_step_solve_twice(built, which):
         iters, resid = C.c_int32(0), C.c_double(0.0)
         st = lib.vebi_ppe_solve_noalloc(
             g["cnt"].data_ptr(), g["col"].data_ptr(), g["val"].data_ptr(), g["diag"].data_ptr(),
-            g["rhs"].data_ptr(), x.data_ptr(), n, n, 1, 1.0e-8, 1000, C.c_void_p(stream.cuda_stream),
+            g["rhs"].data_ptr(), x.data_ptr(), n, n, closed, 1.0e-8, 1000, C.c_void_p(stream.cuda_stream),
             C.byref(iters), C.byref(resid))
         assert st == 0, lib.vebi_last_error()
         got = x.cpu().numpy()
@@ -56,6 +67,18 @@ def test_noalloc_matches_step_solve_twice(built, which):
         # multiply-adds, this one the reference's separate operations): same order, not equal
         assert abs(iters.value - sysm["iters"]) <= max(5, 0.25 * sysm["iters"]), (call, iters.value)
         assert resid.value <= 1e-8 or iters.value > 1000
+    # the asynchronous form: no read-back pointers, so the call only enqueues the solve; the
+    # caller's own stream synchronisation makes x readable
+    x = torch.full((n,), float("nan"), dtype=torch.float64, device=dev)
+    st = lib.vebi_ppe_solve_noalloc(
+        g["cnt"].data_ptr(), g["col"].data_ptr(), g["val"].data_ptr(), g["diag"].data_ptr(),
+        g["rhs"].data_ptr(), x.data_ptr(), n, n, closed, 1.0e-8, 1000, C.c_void_p(stream.cuda_stream),
+        None, None)
+    assert st == 0, lib.vebi_last_error()
+    stream.synchronize()
+    got = x.cpu().numpy()
+    assert np.isfinite(got).all()
+    assert np.abs(got - ref).max() / max(np.abs(ref).max(), 1e-300) < 1e-5
 
 
 def test_noalloc_rejects_oversized_system(built):

@@ -26,7 +26,9 @@ STATUS_NAMES = {
     8: "VEBI_ERR_TIMEOUT",
     9: "VEBI_ERR_NO_DEVICE",
     10: "VEBI_ERR_BOUNDARY",
+    11: "VEBI_ERR_DIVERGED",
 }
+STATUS = {v: k for k, v in STATUS_NAMES.items()}
 WARN_BICGSTAB_BREAKDOWN = 1
 WARN_MAXITER = 2
 WARN_ESCAPEES = 4
@@ -111,7 +113,8 @@ EXPORTED_SYMBOLS = [
     "vebi_batch_create", "vebi_batch_get", "vebi_batch_step", "vebi_batch_destroy", "vebi_set_solver_grid",
     "vebi_dump_async", "vebi_dump_write", "vebi_dump_wait", "vebi_format_list",
     "vebi_set_weissenberg", "vebi_adjoint_create", "vebi_adjoint_record", "vebi_adjoint_replay",
-    "vebi_adjoint_restore", "vebi_adjoint_reverse", "vebi_adjoint_destroy",
+    "vebi_adjoint_restore", "vebi_adjoint_reverse", "vebi_adjoint_destroy", "vebi_test_barrier_timeout",
+    "vebi_set_velocity_limit",
 ]
 DUMP_BACKGROUND = 1
 DUMP_RESTART_READABLE = 2
@@ -166,6 +169,8 @@ def load_library():
     lib.vebi_format_list.argtypes = [C.c_char_p, P(C.c_double), P(C.c_int32), C.c_char_p, C.c_int64]
     lib.vebi_format_list.restype = C.c_int64
     lib.vebi_set_weissenberg.argtypes = [vp, C.c_double]
+    lib.vebi_set_velocity_limit.argtypes = [vp, C.c_double]
+    lib.vebi_set_velocity_limit.restype = C.c_int
     lib.vebi_adjoint_create.argtypes = [vp, C.c_int32, C.c_int32, P(vp)]
     lib.vebi_adjoint_record.argtypes = [vp, C.c_int32, P(VebiStepStats)]
     lib.vebi_adjoint_replay.argtypes = [vp, C.c_int32, P(VebiStepStats)]
@@ -174,6 +179,8 @@ def load_library():
                                          P(C.c_double), P(C.c_double), P(C.c_double), P(C.c_double),
                                          P(C.c_int32)]
     lib.vebi_adjoint_destroy.argtypes = [vp]
+    lib.vebi_test_barrier_timeout.argtypes = [C.c_int32, C.c_int64, P(C.c_int32), P(C.c_double)]
+    lib.vebi_test_barrier_timeout.restype = C.c_int
     for fn in ("vebi_set_weissenberg", "vebi_adjoint_create", "vebi_adjoint_record", "vebi_adjoint_replay",
                "vebi_adjoint_restore", "vebi_adjoint_reverse", "vebi_adjoint_destroy"):
         getattr(lib, fn).restype = C.c_int

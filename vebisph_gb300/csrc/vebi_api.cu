@@ -230,7 +230,7 @@ static int allocate_all(Ctx& x) {
   size_t sel_items = (size_t)(c.npfb > c.mcap ? c.npfb : c.mcap);
   A_(d.sel_blk, sel_items / SEL_CH + 2);
   A_(d.cand, n); A_(d.cand_blk, n / SEL_CH + 2);
-  A_(d.pk, cap);
+  A_(d.pk, cap); A_(d.pko, cap);
   A_(d.ij_count, n); A_(d.ij_link, E);
   A_(d.wGx, E); A_(d.wGy, E); A_(d.wL, E);
   for (int q = 0; q < 4; ++q) A_(d.kgcm[q], n);
@@ -637,6 +637,21 @@ int vebi_set_weissenberg(vebi_ctx* h, double wi) {
   x.c.El = P.El;
   x.c.Wi = P.El * std::sqrt(P.Ra / P.Pr);
   x.c.coeff_polymeric = (1.0 - P.beta) * P.Pr / (P.Ra * P.El);
+  ++x.grid_gen;
+  for (int m = 0; m < 2; ++m) {  // the captured steps hold the old constants
+    if (x.graph[m]) cudaGraphExecDestroy(x.graph[m]);
+    x.graph[m] = nullptr;
+    x.graph_failed[m] = false;
+  }
+  return VEBI_OK;
+}
+
+int vebi_set_velocity_limit(vebi_ctx* h, double u_limit) {
+  if (!h || !(u_limit >= 0.0) || !std::isfinite(u_limit)) return fail(VEBI_ERR_ARG, "bad argument");
+  Ctx& x = h->x;
+  if (x.c.u_limit == u_limit) return VEBI_OK;
+  cudaStreamSynchronize(x.st);
+  x.c.u_limit = u_limit;
   ++x.grid_gen;
   for (int m = 0; m < 2; ++m) {  // the captured steps hold the old constants
     if (x.graph[m]) cudaGraphExecDestroy(x.graph[m]);

@@ -35,6 +35,7 @@ __global__ void k_cell_key(Consts c, Dev d) {
       }
     }
     d.cellpart[k] = key;
+    if (key < 0) d.pk[k] = make_float4(0.f, 0.f, -1.0e6f, -1.0e6f);
   }
 }
 
@@ -156,94 +157,102 @@ __global__ void k_cell_sort(Consts c, Dev d) {
   }
 }
 
-// FP32 offset of each particle to its cell origin, plus its cell coordinates (as floats):
-// pair offsets then need no large coordinate subtracted in FP32
+// FP32 offset of each binned particle to its cell origin, plus its cell coordinates (as
+// floats), by particle (pk) and in cell-list order (pko): pair offsets then need no large
+// coordinate subtracted in FP32.  One thread per cell-list position, after the cell sort.
 __global__ void k_cell_offsets(Consts c, Dev d) {
-  const int np = d.s->np;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < np; k += gridDim.x * blockDim.x) {
-    int key = d.cellpart[k];
-    float4 v = make_float4(0.f, 0.f, -1.0e6f, -1.0e6f);
-    if (key >= 0) {
-      int cx = key % c.ncx, cy = key / c.ncx;
-      double ox = (d.rx[k] - c.x_mint) - (double)cx * c.cell_size;
-      double oy = (d.ry[k] - c.y_mint) - (double)cy * c.cell_size;
-      v = make_float4((float)ox, (float)oy, (float)cx, (float)cy);
-    }
-    d.pk[k] = v;
+  const int tot = d.cell_start[c.nct];
+  for (int pos = blockIdx.x * blockDim.x + threadIdx.x; pos < tot; pos += gridDim.x * blockDim.x) {
+    const int k = d.ip[pos];
+    const int key = d.cellpart[k];
+    const int cx = key % c.ncx, cy = key / c.ncx;
+    const float ox = (float)((d.rx[k] - c.x_mint) - (double)cx * c.cell_size);
+    const float oy = (float)((d.ry[k] - c.y_mint) - (double)cy * c.cell_size);
+    d.pk[k] = make_float4(ox, oy, (float)cx, (float)cy);
+    d.pko[pos] = make_float2(ox, oy);
   }
 }
 
-// pair list: thread per particle, cells in the reference's order, test 0 < r^2 <= 9h^2.
-// The test is decided in FP32 from the cell-relative offsets when it is far from both
-// thresholds, and in FP64 on the reference's expression otherwise.  Error bound of the FP32
-// r^2: offsets are < S (the cell edge) with error <= eps S, the pair offset |r| < 2S gathers
-// at most ~6 eps S, so |r^2_32 - r^2| < ~32 eps S^2 = 32 eps sup_size_2; the band below is
-// 64 eps sup_size_2 (eps = 2^-24), so every pair inside it is re-tested exactly and the list
-// equals the FP64 list.
+// Pair list, 0 < r^2 <= 9h^2, cells in the reference's order C, E, NE, SE, W, NW, SW, N, S
+// (neighbour_finding_mod.F90:261-365), each cell's candidates in its list order.
+//
+// One thread per cell-list position, so a warp holds the particles of two or three adjacent
+// cells and its lanes walk the same candidate lists: every candidate load is a near-broadcast
+// of the cell-ordered offsets (pko), and a candidate's particle index is read only when the
+// pair is taken.  Each list is written to its particle's own column, ij_link[k][i].
+//
+// The test is decided in FP32 when it is far from both thresholds, and in FP64 on the
+// reference's expression otherwise.  Error bound of the FP32 r^2: the offsets are < S (the
+// cell edge) with error <= eps S; a = o_i + d*S (d the cell difference, -1..1) is within 2S
+// and adds eps 2S; a - o_j gathers at most ~6 eps S over |r| < 3S, so |r^2_32 - r^2| < ~40 eps
+// S^2; the band is 64 eps S^2 (eps = 2^-24), so every pair inside it is re-tested exactly and
+// the list equals the FP64 list.  (The reference's last-column quirk, icx = mod(ic, ncx) = 0,
+// pairs the last column with the next row's first cell, ncx-1 cells away: r^2 is then far
+// above the threshold and the FP32 test rejects the whole cell.)
 constexpr int NB_UNROLL = 4;
 
-__global__ void k_neighbours(Consts c, Dev d) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= c.npfb) return;
+__global__ void __launch_bounds__(TPB) k_neighbours(Consts c, Dev d) {
+  const int tot = d.cell_start[c.nct];
+  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
   int cnt = 0;
-  if (!d.inbin[i] && d.cellpart[i] >= 0) {
+  const int i = pos < tot ? d.ip[pos] : c.npfb;
+  if (i < c.npfb) {
     const double xi = d.rx[i], yi = d.ry[i];
-    const float4 pi = d.pk[i];
+    const float2 po = d.pko[pos];
     const float S = (float)c.cell_size;
     const float S2 = (float)c.sup_size_2;
     const float band = 64.0f * 5.9604645e-8f * S2;
-    const int ic = d.cellpart[i] + 1;  // 1-based as the reference
+    const float lo = S2 - band, hi = S2 + band;
+    const int key = d.cellpart[i];
+    const int ic = key + 1;            // 1-based as the reference
     const int icx = ic % c.ncx;        // the reference's column formula: last column -> 0
     const int icy = ic / c.ncx + 1;
-    int jcs[9];
-    int nj = 0;
-    jcs[nj++] = ic;
-    if (icx + 1 <= c.ncx) {
-      jcs[nj++] = ic + 1;
-      if (icy + 1 <= c.ncy) jcs[nj++] = ic + c.ncx + 1;
-      if (icy - 1 >= 1) jcs[nj++] = ic - c.ncx + 1;
-    }
-    if (icx - 1 >= 1) {
-      jcs[nj++] = ic - 1;
-      if (icy + 1 <= c.ncy) jcs[nj++] = ic + c.ncx - 1;
-      if (icy - 1 >= 1) jcs[nj++] = ic - c.ncx - 1;
-    }
-    if (icy + 1 <= c.ncy) jcs[nj++] = ic + c.ncx;
-    if (icy - 1 >= 1) jcs[nj++] = ic - c.ncx;
+    const int cxi = key % c.ncx, cyi = key / c.ncx;
+    const bool e_ok = icx + 1 <= c.ncx, w_ok = icx - 1 >= 1, n_ok = icy + 1 <= c.ncy, s_ok = icy - 1 >= 1;
     bool over = false;
-    for (int q = 0; q < nj; ++q) {
-      int jc = jcs[q];
-      if (jc < 1 || jc > c.nct) continue;  // cells past the grid are empty in the reference
-      int cc = jc - 1;
-      int s0 = __ldg(d.cell_start + cc), s1 = s0 + __ldg(d.cell_cnt + cc);
-      // candidates NB_UNROLL at a time: their index and position loads are issued together
-      for (int jj = s0; jj < s1; jj += NB_UNROLL) {
-        int jv[NB_UNROLL];
-        float4 pv[NB_UNROLL];
+    int* const out = d.ij_link + i;
 #pragma unroll
-        for (int u = 0; u < NB_UNROLL; ++u) jv[u] = jj + u < s1 ? __ldg(d.ip + jj + u) : -1;
+    for (int q = 0; q < 9; ++q) {
+      int jc = ic;
+      bool ok = true;
+      switch (q) {  // C, E, NE, SE, W, NW, SW, N, S
+        case 1: jc = ic + 1; ok = e_ok; break;
+        case 2: jc = ic + c.ncx + 1; ok = e_ok && n_ok; break;
+        case 3: jc = ic - c.ncx + 1; ok = e_ok && s_ok; break;
+        case 4: jc = ic - 1; ok = w_ok; break;
+        case 5: jc = ic + c.ncx - 1; ok = w_ok && n_ok; break;
+        case 6: jc = ic - c.ncx - 1; ok = w_ok && s_ok; break;
+        case 7: jc = ic + c.ncx; ok = n_ok; break;
+        case 8: jc = ic - c.ncx; ok = s_ok; break;
+        default: break;
+      }
+      if (!ok || jc < 1 || jc > c.nct) continue;  // cells past the grid are empty in the reference
+      const int cc = jc - 1;
+      const float ax = po.x + (float)(cxi - cc % c.ncx) * S;
+      const float ay = po.y + (float)(cyi - cc / c.ncx) * S;
+      const int s0 = __ldg(d.cell_start + cc), s1 = s0 + __ldg(d.cell_cnt + cc);
+      for (int jj = s0; jj < s1; jj += NB_UNROLL) {
+        float2 pv[NB_UNROLL];
 #pragma unroll
         for (int u = 0; u < NB_UNROLL; ++u)
-          pv[u] = jv[u] >= 0 ? __ldg(d.pk + jv[u]) : make_float4(0.f, 0.f, 1.0e6f, 1.0e6f);
+          pv[u] = jj + u < s1 ? __ldg(d.pko + jj + u) : make_float2(1.0e6f, 1.0e6f);
 #pragma unroll
         for (int u = 0; u < NB_UNROLL; ++u) {
-          const int j = jv[u];
-          if (j < 0) break;
-          const float4 pj = pv[u];
-          const float f1 = (pi.x - pj.x) + (pi.z - pj.z) * S, f2 = (pi.y - pj.y) + (pi.w - pj.w) * S;
-          const float q = fmaf(f1, f1, f2 * f2);
-          bool take;
-          if (q > S2 + band) take = false;
-          else if (q < S2 - band && q > band) take = true;
-          else {  // near a threshold: the reference's FP64 test
-            double r1 = xi - d.rx[j], r2 = yi - d.ry[j];
-            double rr2 = r1 * r1 + r2 * r2;
-            take = rr2 > 0.0 && rr2 <= c.sup_size_2;
-          }
-          if (take) {
-            if (cnt < c.nplink) d.ij_link[(size_t)cnt * c.npfb + i] = j;
-            else over = true;
-            ++cnt;
+          const float f1 = ax - pv[u].x, f2 = ay - pv[u].y;
+          const float qq = fmaf(f1, f1, f2 * f2);
+          if (qq <= hi) {
+            const int j = __ldg(d.ip + jj + u);
+            bool take = qq < lo && qq > band;
+            if (!take) {  // near a threshold: the reference's FP64 test
+              const double r1 = xi - d.rx[j], r2 = yi - d.ry[j];
+              const double rr2 = r1 * r1 + r2 * r2;
+              take = rr2 > 0.0 && rr2 <= c.sup_size_2;
+            }
+            if (take) {
+              if (cnt < c.nplink) out[(size_t)cnt * c.npfb] = j;
+              else over = true;
+              ++cnt;
+            }
           }
         }
       }
@@ -252,9 +261,11 @@ __global__ void k_neighbours(Consts c, Dev d) {
       set_error(d.s, VEBI_ERR_NEIGH_CAPACITY);
       cnt = c.nplink;
     }
+    d.ij_count[i] = cnt;
   }
-  d.ij_count[i] = cnt;
-  atomicMax(&d.s->maxneigh, cnt);
+  // one atomic per warp for the population maximum
+  for (int o = 16; o > 0; o >>= 1) cnt = max(cnt, __shfl_xor_sync(0xffffffffu, cnt, o));
+  if ((threadIdx.x & 31) == 0 && cnt > 0) atomicMax(&d.s->maxneigh, cnt);
 }
 
 void launch_cells_neighbours(Ctx& x) {
@@ -269,7 +280,9 @@ void launch_cells_neighbours(Ctx& x) {
   VEBI_LAUNCH(x, k_cell_sort, grid_for((long long)c.nct * 32), TPB, c, x.d);
   VEBI_LAUNCH(x, k_cell_offsets, x.gs_blocks, TPB, c, x.d);
   stage_mark(x, 3);
-  VEBI_LAUNCH(x, k_neighbours, grid_for(c.npfb), TPB, c, x.d);
+  // particles outside the cells (in the bin) keep an empty list
+  cudaMemsetAsync(x.d.ij_count, 0, sizeof(int) * (size_t)c.npfb, x.st);
+  VEBI_LAUNCH(x, k_neighbours, grid_for(c.cap), TPB, c, x.d);
 }
 
 }  // namespace vebi

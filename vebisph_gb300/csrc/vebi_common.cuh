@@ -48,6 +48,7 @@ struct Consts {
   int correct_velocity;                             // run correct_velocity (off in the reference)
   int warm_start;                                   // PPE starts from the previous P (opt-in)
   int precond;                                      // 1: multigrid-preconditioned PPE (opt-in)
+  double u_limit;                                   // > 0: velocity bound of the divergence guard
 };
 
 // Scalars that change during a step; they live in device memory so no step needs a host sync.
@@ -146,6 +147,7 @@ struct Dev {
   // with the accuracy of the FP64 difference rounded to FP32
   float2 *hl_u[2], *hl_th, *hl_tau[4], *hl_us[2], *hl_p;
   float4* pk;                                // FP32 offset to the cell origin + cell coords
+  float2* pko;                               // the same offsets in cell-list (ip) order
   float *wGx32, *wGy32, *wL32;               // FP32 pair weights (ELL)
   float* kgcm32[4];
 };

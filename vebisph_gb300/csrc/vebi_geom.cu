@@ -54,7 +54,11 @@ __global__ void k_save_umax(Consts c, Dev d) {
     d.r0y[i] = d.ry[i];
     d.u0x[i] = ux;
     d.u0y[i] = uy;
-    if (i >= c.nbS) um = sqrt(ux * ux + uy * uy);
+    if (i >= c.nbS) {
+      um = sqrt(ux * ux + uy * uy);
+      // divergence guard (opt-in): a non-finite or runaway velocity fails the step
+      if (c.u_limit > 0.0 && !(um <= c.u_limit)) set_error(d.s, VEBI_ERR_DIVERGED);
+    }
   }
   warp_max_pos(&d.s->umax_bits, um);
 }

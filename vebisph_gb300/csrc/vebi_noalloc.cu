@@ -15,6 +15,11 @@
 //    calls that overlap on the GPU (two streams, or two host threads) race on it;
 //  * the first call on a device looks up the array's device address (cudaGetSymbolAddress) with
 //    that device current; make that first call before any stream capture begins.
+//
+// Errors: with iters_out or residual_out given, the call waits for the solve and returns its
+// device-side status (VEBI_ERR_TIMEOUT if a grid barrier gave up).  With both NULL the call only
+// enqueues the work and returns launch errors; a device-side failure then shows in the output,
+// which the kernel fills with NaN.
 #include <mutex>
 #include <string>
 
@@ -92,6 +97,15 @@ __device__ __forceinline__ bool na_sync(NaCtrl* c) {
   return *((volatile int*)&c->error) == 0;
 }
 
+// A block that leaves the solve on an error (a barrier that timed out, or saw another block's
+// timeout) fills its rows of x with NaN, so a failed solve cannot pass for a result even when
+// the caller reads nothing back.  Every block reaches the barrier that failed or returns from
+// it with the error, and the blocks' rows (i = tid, tid + stride, ...) cover 0..n-1.
+__device__ __forceinline__ void na_fail_rows(double* x, int n, int tid, int stride) {
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  for (int i = tid; i < n; i += stride) x[i] = nan;
+}
+
 __device__ __forceinline__ void na_partials(double a, double b, int nval, double* part, double* sh) {
   for (int o = 16; o > 0; o >>= 1) {
     a += __shfl_down_sync(0xffffffffu, a, o);
@@ -161,7 +175,7 @@ __global__ void __launch_bounds__(TPB) k_na_bicgstab(NaArgs a) {
     acc += bi * bi;
   }
   na_partials(acc, 0.0, 1, part + 10 * (size_t)nb, sh);
-  if (!na_sync(ctl)) return;
+  if (!na_sync(ctl)) { na_fail_rows(x, n, tid, stride); return; }
   na_reduce(part + 10 * (size_t)nb, nb, 1, red, shv);
   double rho = red[0], rho0 = 1.0, alpha = 1.0, omega = 1.0, n2r0 = 1.0, n2s0 = 1.0, resid = 0.0;
   int iter = 1, warn = 0;
@@ -177,7 +191,7 @@ __global__ void __launch_bounds__(TPB) k_na_bicgstab(NaArgs a) {
     }
     if (NONULL) {
       na_partials(acc, 0.0, 1, part, sh);
-      if (!na_sync(ctl)) return;
+      if (!na_sync(ctl)) { na_fail_rows(x, n, tid, stride); return; }
       na_reduce(part, nb, 1, red, shv);
       const double mean = red[0] / (double)n;
       for (int i = tid; i < n; i += stride) {
@@ -188,7 +202,7 @@ __global__ void __launch_bounds__(TPB) k_na_bicgstab(NaArgs a) {
     } else {
       for (int i = tid; i < n; i += stride) pinv[i] = p[i] / den(i);
     }
-    if (!na_sync(ctl)) return;
+    if (!na_sync(ctl)) { na_fail_rows(x, n, tid, stride); return; }
     acc = 0.0;
     for (int i = tid; i < n; i += stride) {
       double vi = na_spmv(a, pinv, i);
@@ -196,7 +210,7 @@ __global__ void __launch_bounds__(TPB) k_na_bicgstab(NaArgs a) {
       acc += rb[i] * vi;
     }
     na_partials(acc, 0.0, 1, part + 2 * (size_t)nb, sh);
-    if (!na_sync(ctl)) return;
+    if (!na_sync(ctl)) { na_fail_rows(x, n, tid, stride); return; }
     na_reduce(part + 2 * (size_t)nb, nb, 1, red, shv);
     alpha = rho / (red[0] + 1.0e-15);
     double a2 = 0.0;
@@ -208,7 +222,7 @@ __global__ void __launch_bounds__(TPB) k_na_bicgstab(NaArgs a) {
       a2 += si;
     }
     na_partials(acc, a2, 2, part + 4 * (size_t)nb, sh);
-    if (!na_sync(ctl)) return;
+    if (!na_sync(ctl)) { na_fail_rows(x, n, tid, stride); return; }
     na_reduce(part + 4 * (size_t)nb, nb, 2, red, shv);
     const double n2s = red[0], mean_s = red[1] / (double)n;
     if (iter == 1) n2s0 = (n2s <= small) ? 1.0 : n2s;
@@ -223,7 +237,7 @@ __global__ void __launch_bounds__(TPB) k_na_bicgstab(NaArgs a) {
       if (NONULL) { si = si - mean_s; sv[i] = si; }
       sinv[i] = si / den(i);
     }
-    if (!na_sync(ctl)) return;
+    if (!na_sync(ctl)) { na_fail_rows(x, n, tid, stride); return; }
     acc = 0.0;
     a2 = 0.0;
     for (int i = tid; i < n; i += stride) {
@@ -233,7 +247,7 @@ __global__ void __launch_bounds__(TPB) k_na_bicgstab(NaArgs a) {
       a2 += ti * ti;
     }
     na_partials(acc, a2, 2, part + 6 * (size_t)nb, sh);
-    if (!na_sync(ctl)) return;
+    if (!na_sync(ctl)) { na_fail_rows(x, n, tid, stride); return; }
     na_reduce(part + 6 * (size_t)nb, nb, 2, red, shv);
     omega = red[0] / (red[1] + 1.0e-15);
     acc = 0.0;
@@ -246,7 +260,7 @@ __global__ void __launch_bounds__(TPB) k_na_bicgstab(NaArgs a) {
       a2 += rb[i] * ri;
     }
     na_partials(acc, a2, 2, part + 8 * (size_t)nb, sh);
-    if (!na_sync(ctl)) return;
+    if (!na_sync(ctl)) { na_fail_rows(x, n, tid, stride); return; }
     na_reduce(part + 8 * (size_t)nb, nb, 2, red, shv);
     const double n2r = red[0];
     if (iter == 1) n2r0 = (n2r <= small) ? 1.0 : n2r;
@@ -325,6 +339,15 @@ extern "C" int vebi_ppe_solve_noalloc(const int32_t* ij_count, const int32_t* pp
   long long need = ((long long)n + TPB - 1) / TPB;
   if (need < blocks) blocks = (int)need;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (iters_out || residual_out) {
+    // the read-back waits for the stream, which a stream being captured cannot do
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t ce = cudaStreamIsCapturing(st, &cs);
+    if (ce != cudaSuccess) return na_fail(VEBI_ERR_CUDA, std::string("cudaStreamIsCapturing: ") + cudaGetErrorString(ce));
+    if (cs != cudaStreamCaptureStatusNone)
+      return na_fail(VEBI_ERR_ARG, "vebi_ppe_solve_noalloc: iters_out and residual_out must be NULL while the "
+                                   "stream is being captured (the read-back waits for the stream)");
+  }
   // clear the control words; the vectors are initialised by the kernel itself
   cudaError_t e = cudaMemsetAsync(addr, 0, NA_CTRL * sizeof(double), st);
   if (e != cudaSuccess) return na_fail(VEBI_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));

@@ -565,3 +565,55 @@ void launch_ppe_mixed_solve(Ctx& x) {
 }
 
 }  // namespace vebi
+
+// ---- failure-detection check of the bounded grid barrier ---------------------------------
+// Block 0 never arrives at the barrier, so every other block polls until `limit`, records
+// VEBI_ERR_TIMEOUT in the status word and returns: the wait ends by its own limit and the host
+// reads the status, with the context still usable.  The solvers use the same barrier with the
+// long SPIN_LIMIT.
+namespace vebi {
+__global__ void k_barrier_timeout_check(Scal* s, unsigned long long limit) {
+  if (blockIdx.x == 0) return;
+  grid_sync_bounded(s, limit);
+}
+}  // namespace vebi
+
+extern "C" void vebi_set_last_error_internal(const char* msg);
+
+extern "C" int vebi_test_barrier_timeout(int32_t blocks, int64_t spin_limit, int32_t* status_out, double* ms_out) {
+  using namespace vebi;
+  if (blocks < 2 || blocks > 64 || spin_limit < 1 || spin_limit > (1ll << 22) || !status_out) {
+    vebi_set_last_error_internal("vebi_test_barrier_timeout: blocks in 2..64, spin_limit in 1..2^22, status_out");
+    return VEBI_ERR_ARG;
+  }
+  Scal* s = nullptr;
+  cudaError_t e = cudaMalloc(&s, sizeof(Scal));
+  if (e != cudaSuccess) { vebi_set_last_error_internal(cudaGetErrorString(e)); return VEBI_ERR_CUDA; }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  e = cudaMemset(s, 0, sizeof(Scal));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(32);
+  cfg.stream = 0;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (e == cudaSuccess) e = cudaEventRecord(e0, 0);
+  if (e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, k_barrier_timeout_check, s, (unsigned long long)spin_limit);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, 0);
+  int status = -1;
+  if (e == cudaSuccess) e = cudaMemcpy(&status, &s->error, sizeof(int), cudaMemcpyDeviceToHost);
+  float ms = 0.f;
+  if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(s);
+  if (e != cudaSuccess) { vebi_set_last_error_internal(cudaGetErrorString(e)); return VEBI_ERR_CUDA; }
+  *status_out = status;
+  if (ms_out) *ms_out = ms;
+  return VEBI_OK;
+}

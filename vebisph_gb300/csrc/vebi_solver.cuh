@@ -8,8 +8,10 @@ namespace vebi {
 
 constexpr unsigned long long SPIN_LIMIT = 1ull << 25;  // ~2-4 s of __nanosleep(64) polls
 
-// bounded grid-wide barrier for a co-resident (cooperative) grid; false on error/timeout
-__device__ __forceinline__ bool grid_sync(Scal* s) {
+// bounded grid-wide barrier for a co-resident (cooperative) grid; false on error/timeout.
+// A block that polls more than `limit` times records VEBI_ERR_TIMEOUT and returns false, and so
+// does every block that arrives or polls after the error is recorded.
+__device__ __forceinline__ bool grid_sync_bounded(Scal* s, unsigned long long limit) {
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile unsigned int* vgen = &s->bar_gen;
@@ -25,7 +27,7 @@ __device__ __forceinline__ bool grid_sync(Scal* s) {
       unsigned long long spins = 0;
       while (*vgen == g) {
         if (*verr != 0) break;
-        if (++spins > SPIN_LIMIT) {
+        if (++spins > limit) {
           atomicCAS((int*)&s->error, 0, VEBI_ERR_TIMEOUT);
           break;
         }
@@ -37,6 +39,8 @@ __device__ __forceinline__ bool grid_sync(Scal* s) {
   __syncthreads();
   return *((volatile int*)&s->error) == 0;
 }
+
+__device__ __forceinline__ bool grid_sync(Scal* s) { return grid_sync_bounded(s, SPIN_LIMIT); }
 
 // sum of the block partials of `slot` in a fixed order; identical in every block
 __device__ __forceinline__ void reduce_partials(const double* part, int nb, int nval, double* out,

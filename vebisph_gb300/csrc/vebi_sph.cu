@@ -382,6 +382,8 @@ __global__ void k_pgrad_final(Consts c, Dev d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   double mu = -1.0, mv = -1.0, mp = -1.0;
   if (i < c.npfb) pgrad_one(c, d, i, mu, mv, mp);
+  // divergence guard (opt-in) on the new velocity (false for NaN too)
+  if (c.u_limit > 0.0 && i < c.npfb && !(mu <= c.u_limit && mv <= c.u_limit)) set_error(d.s, VEBI_ERR_DIVERGED);
   warp_max_pos(&d.s->absu_bits, mu);
   warp_max_pos(&d.s->absv_bits, mv);
   warp_max_pos(&d.s->absp_bits, mp);

@@ -295,6 +295,8 @@ __global__ void k_pgrad_final32(Consts c, Dev d) {
     mv = fabs(uy);
     mp = fabs(pi_);
   }
+  // divergence guard (opt-in) on the new velocity (false for NaN too)
+  if (c.u_limit > 0.0 && i < c.npfb && !(mu <= c.u_limit && mv <= c.u_limit)) set_error(d.s, VEBI_ERR_DIVERGED);
   warp_max_pos(&d.s->absu_bits, mu);
   warp_max_pos(&d.s->absv_bits, mv);
   warp_max_pos(&d.s->absp_bits, mp);

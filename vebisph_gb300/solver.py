@@ -154,6 +154,11 @@ class StepSolver:
     def set_weissenberg(self, wi: float):
         self._check(self.lib.vebi_set_weissenberg(self.h, wi), "vebi_set_weissenberg")
 
+    def set_velocity_limit(self, u_limit: float):
+        """Opt-in divergence guard: steps with a non-finite or |u| > u_limit velocity fail
+        with VEBI_ERR_DIVERGED (0 turns it off)."""
+        self._check(self.lib.vebi_set_velocity_limit(self.h, u_limit), "vebi_set_velocity_limit")
+
 
 class Adjoint:
     """Reverse mode of a StepSolver's steps over a window (vebi_adjoint_*).
