@@ -205,16 +205,25 @@ def stage_bandwidth(stage_ms_per_step: dict, n: int, kbar: float, mixed: bool, p
     return out
 
 
-def mg_bytes_per_iteration(n_rows: int, nnz_off: int, n_cells: int, mixed: bool = False) -> float:
-    """Algorithmic bytes of one multigrid-preconditioned BiCGSTAB iteration (closed domain): the
-    unpreconditioned iteration, plus 16 B per row for the mean corrections (row sums), plus two
-    V-cycles.  Particle level of a V-cycle (pre-smoothing only): FP64 12 B per slot + 100 B per
-    row (first sweep 24, residual product 44, restriction 12, prolongation and output 20); mixed
-    8 B per slot + 72 B per row (16, 32, 8, 16).  Coarse levels: ~390 B per cell (the cell
-    level's ELL rows read by the residual and the smoothing sweep, work vectors, and the
+def mg_bytes_per_iteration(n_rows: int, nnz_off: int, n_cells: int, mixed: bool = False,
+                           pairs: float = 5.0) -> float:
+    """Algorithmic bytes of one multigrid-preconditioned BiCGSTAB iteration (closed domain).
+
+    BiCGSTAB vector phases: FP64 168 B per row (p update 32, mean removal 24, s 24, s mean
+    removal 24, x/r update 64), mixed 184 (the same with FP32 (hi, lo) splits of the
+    preconditioned directions); the two products A M^-1 p and A M^-1 s are not separate sparse
+    products: the V-cycle returns w = A M^-1 q, so each costs a pass reading w, the row sum and
+    the dot operand and writing the product, 32 B per row.
+    Two V-cycles.  Particle level (pre-smoothing only): FP64 12 B per slot + 100 B per row (the
+    first sweep 24, the residual product 44, restriction 12, prolongation and output 20), mixed
+    8 B per slot + 72 B per row (16, 32, 8, 16); then w = (q - fr) + gamma (A P) g: q, fr, the
+    row sum, the pair count and w (FP64 36 B, mixed 32 B) plus 12 B per (cell, value) pair of the
+    row beyond its own cell (`pairs` = mean pairs per row).  Coarse levels: ~390 B per cell (the
+    cell level's ELL rows read by the residual and the smoothing sweep, work vectors, and the
     geometric sum of the coarser levels)."""
-    outer = ppe_bytes_per_iteration(n_rows, nnz_off, mixed) + 16.0 * n_rows
+    outer = 2.0 * 32.0 * n_rows + (184.0 if mixed else 168.0) * n_rows
     fine = (8.0 * nnz_off + 72.0 * n_rows) if mixed else (12.0 * nnz_off + 100.0 * n_rows)
+    fine += ((32.0 if mixed else 36.0) + 12.0 * max(pairs - 1.0, 0.0)) * n_rows
     return outer + 2.0 * (fine + 390.0 * n_cells)
 
 
@@ -281,7 +290,8 @@ def run_gb300(args, dist: Dist):
     if mg:
         cp = sol.get("cellpart")[: case.npfb]
         n_cells = int(np.unique(cp[cp >= 0]).size)
-        bytes_iter = mg_bytes_per_iteration(case.npfb, nnz_off, n_cells, mixed=prec == abi.PREC_MIXED)
+        pairs = float(sol.get("mg_pairs").mean())
+        bytes_iter = mg_bytes_per_iteration(case.npfb, nnz_off, n_cells, mixed=prec == abi.PREC_MIXED, pairs=pairs)
     else:
         bytes_iter = ppe_bytes_per_iteration(case.npfb, nnz_off, mixed=prec == abi.PREC_MIXED)
     per_launch_bytes = bytes_iter * iters_per_step
@@ -520,7 +530,8 @@ def run_batch(args, dist: Dist):
     bprec = abi.PREC_MIXED if args.batch_precision == "mixed" else abi.PREC_FP64
     b = BatchSolver(cl, precision=bprec)
     t_create = time.perf_counter() - t0
-    tune = b.autotune(candidates=tuple(int(v) for v in args.tune.split(",")))
+    tune = b.autotune(candidates=tuple(int(v) for v in args.tune.split(",")),
+                      coarse_candidates=(tuple(int(v) for v in args.tune_coarse.split(",")) if mg else (2048,)))
     done = 2 * len(tune["ms_per_candidate"])
     for _ in range(args.warmup):
         b.step(1)
@@ -792,6 +803,8 @@ def main():
     ap.add_argument("--batch-precision", choices=["fp64", "mixed"], default="mixed")
     ap.add_argument("--batch-precond", choices=["none", "multigrid"], default="multigrid")
     ap.add_argument("--tune", default="1,2,4", help="solver rows-per-thread candidates of the batch autotuner")
+    ap.add_argument("--tune-coarse", default="512,2048,8192",
+                    help="coarse-level single-block size candidates of the batch autotuner (multigrid)")
     ap.add_argument("--warm-start", action="store_true",
                     help="opt-in: PPE starts from the previous step's pressure (changes results)")
     ap.add_argument("--adjoint", type=int, default=0,

@@ -278,6 +278,10 @@ int vebi_batch_destroy(vebi_batch* b);
  * ceil(npfb / (256 * rows_per_thread)) blocks, at most the co-resident maximum.  Fewer blocks
  * make a small instance leave room for other instances of a batch.  Re-captures the graph. */
 int vebi_set_solver_grid(vebi_ctx* ctx, int32_t rows_per_thread);
+/* Tile size of the multigrid V-cycle (VEBI_PRECOND_MULTIGRID; no reference counterpart): the
+ * coarse levels of at most `rows` rows run in one thread block with block barriers instead of
+ * across the grid with grid barriers (default 2048).  Results do not depend on it. */
+int vebi_set_coarse_block_rows(vebi_ctx* ctx, int32_t rows);
 
 /* Static description of the library build. */
 const char* vebi_version(void);

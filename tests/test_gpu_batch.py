@@ -42,8 +42,8 @@ def test_batch_equals_individual_runs(built, prec, pc):
 def test_batch_autotune_keeps_results(built):
     from vebisph_gb300.solver import BatchSolver
     b = BatchSolver(_cases()[:3], precision=abi.PREC_MIXED)
-    info = b.autotune(candidates=(1, 4))
-    assert info["rows_per_thread"] in (1, 4)
+    info = b.autotune(candidates=(1, 4), coarse_candidates=(256, 2048))
+    assert info["rows_per_thread"] in (1, 4) and info["coarse_block_rows"] in (256, 2048)
     ms, stats = b.step(1)
     assert all(st["error"] == 0 for st in stats)
     b.close()

@@ -108,3 +108,22 @@ def test_multigrid_with_warm_start_matches_oracle_warm_start(libs):
     assert sg["LS_iters"] < so["LS_iters"]
     gpu.close()
     ref.close()
+
+
+@pytest.mark.parametrize("prec", [abi.PREC_FP64, abi.PREC_MIXED])
+def test_coarse_block_rows_leaves_results_unchanged(libs, prec):
+    """The coarse-level tile size (levels run in one block or across the grid) changes which
+    threads compute each coarse row, not the row's arithmetic: the fields are bit-identical."""
+    StepSolver, _ = libs
+    out = []
+    for rows in (0, 256, 1 << 20):
+        s = StepSolver(_mg(cases.cylinder(2.0e4, Wi=0.6, seed=2)), precision=prec)
+        s.set_coarse_block_rows(rows)
+        for _ in range(3):
+            st = s.step()
+        out.append((st["LS_iters"], {nm: s.get(nm) for nm in ("ux", "uy", "p")}))
+        s.close()
+    for it, f in out[1:]:
+        assert it == out[0][0]
+        for nm in ("ux", "uy", "p"):
+            assert np.array_equal(f[nm], out[0][1][nm]), nm

@@ -114,7 +114,7 @@ EXPORTED_SYMBOLS = [
     "vebi_dump_async", "vebi_dump_write", "vebi_dump_wait", "vebi_format_list",
     "vebi_set_weissenberg", "vebi_adjoint_create", "vebi_adjoint_record", "vebi_adjoint_replay",
     "vebi_adjoint_restore", "vebi_adjoint_reverse", "vebi_adjoint_destroy", "vebi_test_barrier_timeout",
-    "vebi_set_velocity_limit",
+    "vebi_set_velocity_limit", "vebi_set_coarse_block_rows",
 ]
 DUMP_BACKGROUND = 1
 DUMP_RESTART_READABLE = 2
@@ -171,6 +171,8 @@ def load_library():
     lib.vebi_set_weissenberg.argtypes = [vp, C.c_double]
     lib.vebi_set_velocity_limit.argtypes = [vp, C.c_double]
     lib.vebi_set_velocity_limit.restype = C.c_int
+    lib.vebi_set_coarse_block_rows.argtypes = [vp, C.c_int32]
+    lib.vebi_set_coarse_block_rows.restype = C.c_int
     lib.vebi_adjoint_create.argtypes = [vp, C.c_int32, C.c_int32, P(vp)]
     lib.vebi_adjoint_record.argtypes = [vp, C.c_int32, P(VebiStepStats)]
     lib.vebi_adjoint_replay.argtypes = [vp, C.c_int32, P(VebiStepStats)]

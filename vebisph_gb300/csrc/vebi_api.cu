@@ -273,8 +273,9 @@ static int allocate_all(Ctx& x) {
     }
     A_(x.d_mg, x.mg.size());
     cudaMemcpy(x.d_mg, x.mg.data(), sizeof(MgLevel) * x.mg.size(), cudaMemcpyHostToDevice);
-    A_(x.mg_z, n); A_(x.mg_fr, n); A_(x.mg_dinv0, n); A_(x.mg_rsum, n);
+    A_(x.mg_z, n); A_(x.mg_fr, n); A_(x.mg_dinv0, n); A_(x.mg_rsum, n); A_(x.mg_w, n);
     A_(x.mg_ragg, n * MG_ROW_SLOTS); A_(x.mg_rval, n * MG_ROW_SLOTS); A_(x.mg_rcnt, n);
+    A_(x.mg_kinv, (size_t)MG_COARSEST * MG_COARSEST); A_(x.mg_kinv_ok, 1);
   }
 #undef A_
   return VEBI_OK;
@@ -628,6 +629,21 @@ int vebi_set_solver_grid(vebi_ctx* h, int32_t rows_per_thread) {
   return VEBI_OK;
 }
 
+int vebi_set_coarse_block_rows(vebi_ctx* h, int32_t rows) {
+  if (!h || rows < 0) return fail(VEBI_ERR_ARG, "bad argument");
+  Ctx& x = h->x;
+  if (x.mg_block_rows == rows) return VEBI_OK;
+  cudaStreamSynchronize(x.st);
+  x.mg_block_rows = rows;
+  ++x.grid_gen;
+  for (int m = 0; m < 2; ++m) {  // the captured steps hold the old launch arguments
+    if (x.graph[m]) cudaGraphExecDestroy(x.graph[m]);
+    x.graph[m] = nullptr;
+    x.graph_failed[m] = false;
+  }
+  return VEBI_OK;
+}
+
 int vebi_set_weissenberg(vebi_ctx* h, double wi) {
   if (!h || !(wi > 0.0)) return fail(VEBI_ERR_ARG, "bad argument");
   Ctx& x = h->x;
@@ -933,6 +949,7 @@ static DView dview(Ctx& x, const std::string& nm) {
   if (nm == "grad_py") return D(d.gpy, n);
   if (nm == "conc" && d.conc) return D(d.conc, n);
   if (nm == "div_r" && d.div_r) return D(d.div_r, n);
+  if (nm == "mg_pairs" && x.mg_rcnt) return I(x.mg_rcnt, n);  // (cell, value) pairs of each row of A P
   return DView{nullptr, 0, -1};
 }
 

@@ -169,7 +169,7 @@ __global__ void k_cell_offsets(Consts c, Dev d) {
     const float ox = (float)((d.rx[k] - c.x_mint) - (double)cx * c.cell_size);
     const float oy = (float)((d.ry[k] - c.y_mint) - (double)cy * c.cell_size);
     d.pk[k] = make_float4(ox, oy, (float)cx, (float)cy);
-    d.pko[pos] = make_float2(ox, oy);
+    d.pko[pos] = make_float4(ox, oy, __int_as_float(k), 0.f);
   }
 }
 
@@ -178,8 +178,8 @@ __global__ void k_cell_offsets(Consts c, Dev d) {
 //
 // One thread per cell-list position, so a warp holds the particles of two or three adjacent
 // cells and its lanes walk the same candidate lists: every candidate load is a near-broadcast
-// of the cell-ordered offsets (pko), and a candidate's particle index is read only when the
-// pair is taken.  Each list is written to its particle's own column, ij_link[k][i].
+// of the cell-ordered record (pko: offsets and particle index in one 16-byte load).  Each
+// list is written to its particle's own column, ij_link[k][i].
 //
 // The test is decided in FP32 when it is far from both thresholds, and in FP64 on the
 // reference's expression otherwise.  Error bound of the FP32 r^2: the offsets are < S (the
@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(TPB) k_neighbours(Consts c, Dev d) {
   const int i = pos < tot ? d.ip[pos] : c.npfb;
   if (i < c.npfb) {
     const double xi = d.rx[i], yi = d.ry[i];
-    const float2 po = d.pko[pos];
+    const float4 po = d.pko[pos];
     const float S = (float)c.cell_size;
     const float S2 = (float)c.sup_size_2;
     const float band = 64.0f * 5.9604645e-8f * S2;
@@ -211,37 +211,33 @@ __global__ void __launch_bounds__(TPB) k_neighbours(Consts c, Dev d) {
     const bool e_ok = icx + 1 <= c.ncx, w_ok = icx - 1 >= 1, n_ok = icy + 1 <= c.ncy, s_ok = icy - 1 >= 1;
     bool over = false;
     int* const out = d.ij_link + i;
-#pragma unroll
+    // the nine cells C, E, NE, SE, W, NW, SW, N, S as (dx + 1, dy + 1) in two bits each; the
+    // loop stays rolled (the kernel is bound by instruction fetch when it is unrolled)
+    constexpr unsigned DXP = (1u << 0) | (2u << 2) | (2u << 4) | (2u << 6) | (0u << 8) | (0u << 10) | (0u << 12) |
+                             (1u << 14) | (1u << 16);
+    constexpr unsigned DYP = (1u << 0) | (1u << 2) | (2u << 4) | (0u << 6) | (1u << 8) | (2u << 10) | (0u << 12) |
+                             (2u << 14) | (0u << 16);
+#pragma unroll 1
     for (int q = 0; q < 9; ++q) {
-      int jc = ic;
-      bool ok = true;
-      switch (q) {  // C, E, NE, SE, W, NW, SW, N, S
-        case 1: jc = ic + 1; ok = e_ok; break;
-        case 2: jc = ic + c.ncx + 1; ok = e_ok && n_ok; break;
-        case 3: jc = ic - c.ncx + 1; ok = e_ok && s_ok; break;
-        case 4: jc = ic - 1; ok = w_ok; break;
-        case 5: jc = ic + c.ncx - 1; ok = w_ok && n_ok; break;
-        case 6: jc = ic - c.ncx - 1; ok = w_ok && s_ok; break;
-        case 7: jc = ic + c.ncx; ok = n_ok; break;
-        case 8: jc = ic - c.ncx; ok = s_ok; break;
-        default: break;
-      }
+      const int dxq = (int)((DXP >> (2 * q)) & 3u) - 1, dyq = (int)((DYP >> (2 * q)) & 3u) - 1;
+      const bool ok = (dxq != 1 || e_ok) && (dxq != -1 || w_ok) && (dyq != 1 || n_ok) && (dyq != -1 || s_ok);
+      const int jc = ic + dxq + dyq * c.ncx;
       if (!ok || jc < 1 || jc > c.nct) continue;  // cells past the grid are empty in the reference
       const int cc = jc - 1;
       const float ax = po.x + (float)(cxi - cc % c.ncx) * S;
       const float ay = po.y + (float)(cyi - cc / c.ncx) * S;
       const int s0 = __ldg(d.cell_start + cc), s1 = s0 + __ldg(d.cell_cnt + cc);
       for (int jj = s0; jj < s1; jj += NB_UNROLL) {
-        float2 pv[NB_UNROLL];
+        float4 pv[NB_UNROLL];
 #pragma unroll
         for (int u = 0; u < NB_UNROLL; ++u)
-          pv[u] = jj + u < s1 ? __ldg(d.pko + jj + u) : make_float2(1.0e6f, 1.0e6f);
+          pv[u] = jj + u < s1 ? __ldg(d.pko + jj + u) : make_float4(1.0e6f, 1.0e6f, 0.f, 0.f);
 #pragma unroll
         for (int u = 0; u < NB_UNROLL; ++u) {
           const float f1 = ax - pv[u].x, f2 = ay - pv[u].y;
           const float qq = fmaf(f1, f1, f2 * f2);
           if (qq <= hi) {
-            const int j = __ldg(d.ip + jj + u);
+            const int j = __float_as_int(pv[u].z);
             bool take = qq < lo && qq > band;
             if (!take) {  // near a threshold: the reference's FP64 test
               const double r1 = xi - d.rx[j], r2 = yi - d.ry[j];

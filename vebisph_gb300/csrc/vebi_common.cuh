@@ -147,7 +147,8 @@ struct Dev {
   // with the accuracy of the FP64 difference rounded to FP32
   float2 *hl_u[2], *hl_th, *hl_tau[4], *hl_us[2], *hl_p;
   float4* pk;                                // FP32 offset to the cell origin + cell coords
-  float2* pko;                               // the same offsets in cell-list (ip) order
+  float4* pko;                               // the same offsets in cell-list (ip) order, with the
+                                             // particle index (bits of .z); .w unused
   float *wGx32, *wGy32, *wL32;               // FP32 pair weights (ELL)
   float* kgcm32[4];
 };

@@ -32,6 +32,7 @@ struct Ctx {
   int coop_blocks = 0;       // persistent PPE grid (co-resident blocks)
   int coop_blocks_mixed = 0; // same for the mixed-precision solver
   int solver_rows_per_thread = 1;  // batch tuning: rows per solver thread
+  int mg_block_rows = MG_BLOCK_ROWS;  // batch tuning: coarse levels of at most this many rows run in one block
   int grid_gen = 0;                // bumped when a launch shape changes (captured graphs are stale)
   int gs_blocks = 0;         // grid of grid-stride kernels over dynamic counts
   int sel_max_blocks = 0;    // blocks of the ordered-select kernels
@@ -41,8 +42,10 @@ struct Ctx {
   std::vector<MgLevel> mg;         // coarse levels, finest first
   MgLevel* d_mg = nullptr;         // device copy of the level descriptors
   int mg_blocks = 0;               // co-resident blocks of the preconditioned solver
-  double *mg_z = nullptr, *mg_fr = nullptr, *mg_dinv0 = nullptr, *mg_rsum = nullptr;
+  double *mg_z = nullptr, *mg_fr = nullptr, *mg_dinv0 = nullptr, *mg_rsum = nullptr, *mg_w = nullptr;
   int *mg_ragg = nullptr, *mg_rcnt = nullptr;  // per-row (cell, value) pairs of the level-1 build
+  double* mg_kinv = nullptr;       // dense inverse of the coarsest level
+  int* mg_kinv_ok = nullptr;
   double* mg_rval = nullptr;
   std::vector<void*> allocs;
   DumpState* dump = nullptr;       // output staging (vebi_output.cu), made at the first dump

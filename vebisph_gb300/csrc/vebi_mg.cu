@@ -179,6 +179,83 @@ __global__ void k_mg_coarsen(MgLevel F, MgLevel G, Scal* s) {
   if (!ok) s->mg_fail = 1;
 }
 
+// The coarsest level's dense inverse, for a direct coarse solve in the V-cycle: Gauss-Jordan
+// with partial pivoting in one warp, row r in lane r (at most MG_COARSEST = 32 rows).  A
+// closed domain's coarse matrix is singular (its rows sum to zero: the constant is in its null
+// space), so it is inverted as M + alpha 1 1^T with alpha = mean |diag| / n, which moves that
+// eigenvalue to mean |diag| and leaves the mean-free solution of M x = b unchanged.  *ok = 0
+// (a zero pivot, or a level too large) makes the V-cycle fall back to Jacobi sweeps.
+__global__ void __launch_bounds__(32) k_mg_coarse_inverse(MgLevel K, double* inv, int* ok, int closed) {
+  __shared__ double M[MG_COARSEST][2 * MG_COARSEST + 1];
+  const int n = K.n, r = threadIdx.x;
+  if (n > MG_COARSEST || n < 1) {
+    if (r == 0) *ok = 0;
+    return;
+  }
+  double ad = r < n ? fabs(K.diag[r]) : 0.0;
+  for (int o = 16; o > 0; o >>= 1) ad += __shfl_xor_sync(0xffffffffu, ad, o);
+  const double alpha = closed ? ad / ((double)n * (double)n) : 0.0;
+  if (r < n) {
+    for (int c = 0; c < 2 * n; ++c) M[r][c] = (c < n ? alpha : 0.0);
+    M[r][r] += K.diag[r];
+    M[r][n + r] = 1.0;
+    const int m = K.cnt[r];
+    for (int t = 0; t < m; ++t) M[r][K.col[(size_t)t * K.n + r]] += K.val[(size_t)t * K.n + r];
+  }
+  __syncwarp();
+  bool good = true;
+  for (int k = 0; k < n; ++k) {
+    double v = (r >= k && r < n) ? fabs(M[r][k]) : -1.0;
+    int p = r;
+    for (int o = 16; o > 0; o >>= 1) {  // argmax, ties to the lower row
+      const double v2 = __shfl_xor_sync(0xffffffffu, v, o);
+      const int p2 = __shfl_xor_sync(0xffffffffu, p, o);
+      if (v2 > v || (v2 == v && p2 < p)) { v = v2; p = p2; }
+    }
+    if (!(v > 0.0)) { good = false; break; }
+    if (p != k)
+      for (int c = r; c < 2 * n; c += 32) { const double t = M[k][c]; M[k][c] = M[p][c]; M[p][c] = t; }
+    __syncwarp();
+    const double piv = M[k][k];
+    __syncwarp();
+    for (int c = r; c < 2 * n; c += 32) M[k][c] /= piv;
+    __syncwarp();
+    if (r < n && r != k) {
+      const double f = M[r][k];
+      for (int c = 0; c < 2 * n; ++c) M[r][c] = fma(-f, M[k][c], M[r][c]);
+    }
+    __syncwarp();
+  }
+  if (good && r < n)
+    for (int c = 0; c < n; ++c) inv[(size_t)r * n + c] = M[r][n + c];
+  if (r == 0) *ok = good ? 1 : 0;
+}
+
+// sum over a row's cell pairs t = 1..m-1 of (A P)_ic (g_c - g_own), in pair order.  The pairs
+// are taken four at a time with all their loads issued before the gathers of g they index,
+// so a row costs one or two dependent round trips instead of two per pair.
+__device__ __forceinline__ double ap_pairs(const int* __restrict__ ragg, const double* __restrict__ rval, int m,
+                                           size_t i, size_t n, const double* g, double gc, double ap) {
+  for (int t0 = 1; t0 < m; t0 += 4) {
+    int c4[4];
+    double v4[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const bool ok = t0 + u < m;
+      const size_t e = (size_t)(t0 + u) * n + i;
+      c4[u] = ok ? __ldg(ragg + e) : -1;
+      v4[u] = ok ? __ldg(rval + e) : 0.0;
+    }
+    double g4[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) g4[u] = c4[u] >= 0 ? g[c4[u]] : gc;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (c4[u] >= 0) ap = fma(v4[u], g4[u] - gc, ap);
+  }
+  return ap;
+}
+
 // ---------------------------------------------------------------- V-cycle
 struct MgArgs {
   BiArgs b;                  // the unpreconditioned solver's arguments
@@ -187,6 +264,13 @@ struct MgArgs {
   int tail;                  // first level handled by block 0 alone
   const int *agg, *cstart, *ccnt, *ip;  // fine aggregate (cell) of each row; cell lists
   double *z, *fr, *dinv0, *rsum;        // fine work vectors, 1/diag, row sums
+  // A P by fine row: (cell, sum of the row's values in that cell) pairs, own cell first
+  // (k_mg_rows), and A times the V-cycle's output
+  const int *ragg, *rcnt;
+  const double* rval;
+  double* w;
+  const double* kinv;        // the coarsest level's dense inverse, if *kinv_ok
+  const int* kinv_ok;
 };
 
 // (A x)_c on a coarse level; x may have been written by other blocks in this launch
@@ -244,11 +328,20 @@ __device__ void mg_block_levels(const MgArgs& a) {
     __syncthreads();
   }
   const MgLevel K = a.lv[a.nl - 1];
-  for (int sw = 0; sw < MG_SWEEPS; ++sw) {
-    lv_smooth(K, i0, st);
+  if (a.kinv_ok && *a.kinv_ok) {  // direct solve with the dense inverse
+    for (int r = i0; r < K.n; r += st) {
+      double v = 0.0;
+      for (int c = 0; c < K.n; ++c) v = fma(__ldg(a.kinv + (size_t)r * K.n + c), K.b[c], v);
+      K.x[r] = v;
+    }
     __syncthreads();
-    for (int c = i0; c < K.n; c += st) K.x[c] = K.r[c];
-    __syncthreads();
+  } else {
+    for (int sw = 0; sw < MG_SWEEPS; ++sw) {
+      lv_smooth(K, i0, st);
+      __syncthreads();
+      for (int c = i0; c < K.n; c += st) K.x[c] = K.r[c];
+      __syncthreads();
+    }
   }
   for (int l = a.nl - 2; l >= a.tail; --l) {
     const MgLevel F = a.lv[l];
@@ -261,12 +354,25 @@ __device__ void mg_block_levels(const MgArgs& a) {
 
 // out = M^-1 q by one V-cycle; the last loop also writes the block partial of sum(out) into
 // slot.  q needs only its own rows complete (the calling thread wrote them).
-__device__ bool mg_vcycle(const MgArgs& a, const double* q, double* out, double* slot, double* sh, int tid,
-                          int stride) {
+// q -= qshift first (the closed domain's mean removal), stored back.  As in the mixed solver,
+// the vector passes take rows i and i + stride per thread and issue their loads first.
+__device__ bool mg_vcycle(const MgArgs& a, double* q, double qshift, double* out, double* slot, double* sh,
+                          int tid, int stride) {
   const int n = a.b.n;
   Scal* s = a.b.sc;
   double* z = a.z;
-  for (int i = tid; i < n; i += stride) z[i] = MG_OMEGA * a.dinv0[i] * q[i];
+  for (int i = tid; i < n; i += 2 * stride) {
+    const int j = i + stride;
+    const bool h = j < n;
+    const double qi = q[i] - qshift, qj = h ? q[j] - qshift : 0.0;
+    const double di = a.dinv0[i], dj = h ? a.dinv0[j] : 0.0;
+    q[i] = qi;
+    z[i] = MG_OMEGA * di * qi;
+    if (h) {
+      q[j] = qj;
+      z[j] = MG_OMEGA * dj * qj;
+    }
+  }
   if (!grid_sync(s)) return false;
   for (int i = tid; i < n; i += stride) a.fr[i] = q[i] - spmv_row(a.b, z, i);
   if (!grid_sync(s)) return false;
@@ -301,13 +407,24 @@ __device__ bool mg_vcycle(const MgArgs& a, const double* q, double* out, double*
     lv_smooth(F, tid, stride);
     if (!grid_sync(s)) return false;
   }
-  // prolongation to the particles (the particle level is pre-smoothed only)
+  // prolongation to the particles (the particle level is pre-smoothed only), and
+  // w = A out = A z + gamma (A P) g1 with A z = q - fr from the fine residual and (A P) g1 in
+  // difference form over the row's cell pairs: rowsum_i g_own + sum_c (AP)_ic (g_c - g_own)
   const double* g1 = lv_sol(a, 0);
   double acc = 0.0;
   for (int i = tid; i < n; i += stride) {
     const int c = __ldg(a.agg + i);
-    const double o = c >= 0 ? fma(MG_GAMMA, g1[c], z[i]) : z[i];
+    const double zi = z[i], qi = q[i], fri = a.fr[i];
+    double o = zi;
+    double w = qi - fri;
+    if (c >= 0) {
+      const double gc = g1[c];
+      o = fma(MG_GAMMA, gc, o);
+      const double ap = ap_pairs(a.ragg, a.rval, __ldg(a.rcnt + i), i, n, g1, gc, a.rsum[i] * gc);
+      w = fma(MG_GAMMA, ap, w);
+    }
     out[i] = o;
+    a.w[i] = w;
     acc += o;
   }
   write_partials(acc, 0.0, 1, slot, sh);
@@ -332,12 +449,15 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
   const double small = NONULL ? 1.0e-6 : 4.0;  // open solver: the integer expression 10-6
   double red[2];
   double acc = 0.0;
-  // out = M^-1 q (q: own rows complete) and the block partial of sum(out) into slot
-  auto precond = [&](const double* q, double* out, double* slot) -> bool {
-    if (use_mg) return mg_vcycle(m, q, out, slot, sh, tid, stride);
+  // out = M^-1 (q - qshift) with q -= qshift stored back (q: own rows complete), and the
+  // block partial of sum(out) into slot
+  auto precond = [&](double* q, double qshift, double* out, double* slot) -> bool {
+    if (use_mg) return mg_vcycle(m, q, qshift, out, slot, sh, tid, stride);
     double sum = 0.0;
     for (int i = tid; i < n; i += stride) {
-      const double o = NONULL ? q[i] * rinv1 : q[i] * a.rinvM[i];
+      const double qi = q[i] - qshift;
+      q[i] = qi;
+      const double o = NONULL ? qi * rinv1 : qi * a.rinvM[i];
       out[i] = o;
       sum += o;
     }
@@ -382,29 +502,55 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
     if (rho == 0.0) { warn |= VEBI_WARN_BICGSTAB_BREAKDOWN; done = true; break; }
     const double beta = rho / (rho0 + 1.0e-15) * alpha / (omega + 1.0e-15);
     acc = 0.0;
-    for (int i = tid; i < n; i += stride) {
-      double pi = (iter == 1) ? a.r[i] : fma(beta, fma(-omega, a.v[i], a.p[i]), a.r[i]);
-      a.p[i] = pi;
-      acc += pi;
+    for (int i = tid; i < n; i += 2 * stride) {
+      const int j = i + stride;
+      const bool h = j < n;
+      const double ri = a.r[i], vi = a.v[i], pi = a.p[i];
+      const double rj = h ? a.r[j] : 0.0, vj = h ? a.v[j] : 0.0, pj = h ? a.p[j] : 0.0;
+      const double ni = (iter == 1) ? ri : fma(beta, fma(-omega, vi, pi), ri);
+      a.p[i] = ni;
+      acc += ni;
+      if (h) {
+        const double nj = (iter == 1) ? rj : fma(beta, fma(-omega, vj, pj), rj);
+        a.p[j] = nj;
+        acc += nj;
+      }
     }
+    double mean = 0.0;
     if (NONULL) {
       write_partials(acc, 0.0, 1, part, sh);
       if (!grid_sync(s)) return;
       reduce_partials(part, nb, 1, red, shv);
-      const double mean = red[0] / (double)n;
-      for (int i = tid; i < n; i += stride) a.p[i] = a.p[i] - mean;
+      mean = red[0] / (double)n;
     }
-    // p_hat = M^-1 p, made mean-free (closed domains) through mp
-    if (!precond(a.p, a.pinv, part + 1 * (size_t)nb)) return;
+    // p_hat = M^-1 (p - mean), made mean-free (closed domains) through mp
+    if (!precond(a.p, mean, a.pinv, part + 1 * (size_t)nb)) return;
     if (!grid_sync(s)) return;
     reduce_partials(part + 1 * (size_t)nb, nb, 1, red, shv);
     const double mp = NONULL ? red[0] / (double)n : 0.0;
     // v = A (p_hat - mp) ; (r_bar, v)
     acc = 0.0;
-    for (int i = tid; i < n; i += stride) {
-      double vi = fma(-mp, m.rsum[i], spmv_row(a, a.pinv, i));
-      a.v[i] = vi;
-      acc = fma(a.rb[i], vi, acc);
+    if (use_mg) {
+      for (int i = tid; i < n; i += 2 * stride) {
+        const int j = i + stride;
+        const bool h = j < n;
+        const double wi = m.w[i], rsi = m.rsum[i], rbi = a.rb[i];
+        const double wj = h ? m.w[j] : 0.0, rsj = h ? m.rsum[j] : 0.0, rbj = h ? a.rb[j] : 0.0;
+        const double vi = fma(-mp, rsi, wi);
+        a.v[i] = vi;
+        acc = fma(rbi, vi, acc);
+        if (h) {
+          const double vj = fma(-mp, rsj, wj);
+          a.v[j] = vj;
+          acc = fma(rbj, vj, acc);
+        }
+      }
+    } else {
+      for (int i = tid; i < n; i += stride) {
+        double vi = fma(-mp, m.rsum[i], spmv_row(a, a.pinv, i));
+        a.v[i] = vi;
+        acc = fma(a.rb[i], vi, acc);
+      }
     }
     write_partials(acc, 0.0, 1, part + 2 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
@@ -412,11 +558,21 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
     alpha = rho / (red[0] + 1.0e-15);
     double a2 = 0.0;
     acc = 0.0;
-    for (int i = tid; i < n; i += stride) {
-      double si = fma(-alpha, a.v[i], a.r[i]);
+    for (int i = tid; i < n; i += 2 * stride) {
+      const int j = i + stride;
+      const bool h = j < n;
+      const double vi = a.v[i], ri = a.r[i];
+      const double vj = h ? a.v[j] : 0.0, rj = h ? a.r[j] : 0.0;
+      const double si = fma(-alpha, vi, ri);
       a.s[i] = si;
       acc = fma(si, si, acc);
       a2 += si;
+      if (h) {
+        const double sj = fma(-alpha, vj, rj);
+        a.s[j] = sj;
+        acc = fma(sj, sj, acc);
+        a2 += sj;
+      }
     }
     write_partials(acc, a2, 2, part + 4 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
@@ -430,20 +586,37 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
       done = true;
       break;
     }
-    if (NONULL)
-      for (int i = tid; i < n; i += stride) a.s[i] = a.s[i] - mean_s;
-    if (!precond(a.s, a.sinv, part + 3 * (size_t)nb)) return;
+    if (!precond(a.s, NONULL ? mean_s : 0.0, a.sinv, part + 3 * (size_t)nb)) return;
     if (!grid_sync(s)) return;
     reduce_partials(part + 3 * (size_t)nb, nb, 1, red, shv);
     const double ms = NONULL ? red[0] / (double)n : 0.0;
     // t = A (s_hat - ms) ; (t, s) ; |t|^2
     acc = 0.0;
     a2 = 0.0;
-    for (int i = tid; i < n; i += stride) {
-      double ti = fma(-ms, m.rsum[i], spmv_row(a, a.sinv, i));
-      a.t[i] = ti;
-      acc = fma(ti, a.s[i], acc);
-      a2 = fma(ti, ti, a2);
+    if (use_mg) {
+      for (int i = tid; i < n; i += 2 * stride) {
+        const int j = i + stride;
+        const bool h = j < n;
+        const double wi = m.w[i], rsi = m.rsum[i], si = a.s[i];
+        const double wj = h ? m.w[j] : 0.0, rsj = h ? m.rsum[j] : 0.0, sj = h ? a.s[j] : 0.0;
+        const double ti = fma(-ms, rsi, wi);
+        a.t[i] = ti;
+        acc = fma(ti, si, acc);
+        a2 = fma(ti, ti, a2);
+        if (h) {
+          const double tj = fma(-ms, rsj, wj);
+          a.t[j] = tj;
+          acc = fma(tj, sj, acc);
+          a2 = fma(tj, tj, a2);
+        }
+      }
+    } else {
+      for (int i = tid; i < n; i += stride) {
+        double ti = fma(-ms, m.rsum[i], spmv_row(a, a.sinv, i));
+        a.t[i] = ti;
+        acc = fma(ti, a.s[i], acc);
+        a2 = fma(ti, ti, a2);
+      }
     }
     write_partials(acc, a2, 2, part + 6 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
@@ -451,12 +624,24 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
     omega = red[0] / (red[1] + 1.0e-15);
     acc = 0.0;
     a2 = 0.0;
-    for (int i = tid; i < n; i += stride) {
-      a.x[i] = fma(omega, a.sinv[i] - ms, fma(alpha, a.pinv[i] - mp, a.x[i]));
-      double ri = fma(-omega, a.t[i], a.s[i]);
+    for (int i = tid; i < n; i += 2 * stride) {
+      const int j = i + stride;
+      const bool h = j < n;
+      const double sii = a.sinv[i], pii = a.pinv[i], xi = a.x[i], ti = a.t[i], s_i = a.s[i], rbi = a.rb[i];
+      const double sij = h ? a.sinv[j] : 0.0, pij = h ? a.pinv[j] : 0.0, xj = h ? a.x[j] : 0.0;
+      const double tj = h ? a.t[j] : 0.0, s_j = h ? a.s[j] : 0.0, rbj = h ? a.rb[j] : 0.0;
+      a.x[i] = fma(omega, sii - ms, fma(alpha, pii - mp, xi));
+      const double ri = fma(-omega, ti, s_i);
       a.r[i] = ri;
       acc = fma(ri, ri, acc);
-      a2 = fma(a.rb[i], ri, a2);
+      a2 = fma(rbi, ri, a2);
+      if (h) {
+        a.x[j] = fma(omega, sij - ms, fma(alpha, pij - mp, xj));
+        const double rj = fma(-omega, tj, s_j);
+        a.r[j] = rj;
+        acc = fma(rj, rj, acc);
+        a2 = fma(rbj, rj, a2);
+      }
     }
     write_partials(acc, a2, 2, part + 8 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
@@ -491,6 +676,11 @@ struct MgMxArgs {
   int nl, tail;
   const int *agg, *cstart, *ccnt, *ip;
   float *z, *fr, *dinv0;
+  const int *ragg, *rcnt;  // A P by fine row, as in MgArgs
+  const double* rval;
+  double* w;               // A times the V-cycle's output
+  const double* kinv;      // the coarsest level's dense inverse, if *kinv_ok
+  const int* kinv_ok;
 };
 
 // sum_k A_ik (z_col - z_i) + rowsum_i z_i in FP32 (one FP32 vector)
@@ -521,12 +711,27 @@ __device__ __forceinline__ float spmv_diff32s(const MxArgs& a, const float* z, i
 }
 
 // out = M^-1 q as FP32 (hi, lo) pairs; block partial of sum(out) into slot
-__device__ bool mg_vcycle_mixed(const MgMxArgs& a, const double* q, float2* out, double* slot, double* sh,
-                                int tid, int stride) {
+// The vector passes of this solver take two rows per thread per pass, i and i + stride (the
+// rows each thread owns stay the same), and issue all of a pass's loads before its stores: the
+// compiler cannot move a load above a store to another array it may alias.
+__device__ bool mg_vcycle_mixed(const MgMxArgs& a, double* q, double qshift, float2* out, double* slot,
+                                double* sh, int tid, int stride) {
   const int n = a.b.n;
   Scal* s = a.b.sc;
   float* z = a.z;
-  for (int i = tid; i < n; i += stride) z[i] = (float)MG_OMEGA * a.dinv0[i] * (float)q[i];
+  // q -= qshift (the closed domain's mean removal), then z = omega D^-1 q
+  for (int i = tid; i < n; i += 2 * stride) {
+    const int j = i + stride;
+    const bool h = j < n;
+    const double qi = q[i] - qshift, qj = h ? q[j] - qshift : 0.0;
+    const float di = a.dinv0[i], dj = h ? a.dinv0[j] : 0.f;
+    q[i] = qi;
+    z[i] = (float)MG_OMEGA * di * (float)qi;
+    if (h) {
+      q[j] = qj;
+      z[j] = (float)MG_OMEGA * dj * (float)qj;
+    }
+  }
   if (!grid_sync(s)) return false;
   for (int i = tid; i < n; i += stride) a.fr[i] = (float)q[i] - spmv_diff32s(a.b, z, i);
   if (!grid_sync(s)) return false;
@@ -549,6 +754,8 @@ __device__ bool mg_vcycle_mixed(const MgMxArgs& a, const double* q, float2* out,
   c.lv = a.lv;
   c.nl = a.nl;
   c.tail = a.tail;
+  c.kinv = a.kinv;
+  c.kinv_ok = a.kinv_ok;
   for (int l = 0; l < a.tail; ++l) {
     const MgLevel F = a.lv[l], G = a.lv[l + 1];
     lv_residual(F, tid, stride);
@@ -565,13 +772,25 @@ __device__ bool mg_vcycle_mixed(const MgMxArgs& a, const double* q, float2* out,
     lv_smooth(F, tid, stride);
     if (!grid_sync(s)) return false;
   }
-  // prolongation to the particles (pre-smoothed only), output as FP32 (hi, lo) pairs
+  // prolongation to the particles (pre-smoothed only), output as FP32 (hi, lo) pairs, and
+  // w = A out as in the FP64 V-cycle: A z = q - fr (q as rounded to FP32 for fr), plus
+  // gamma (A P) g1 in difference form with the mixed operator's row sums
   const double* g1 = lv_sol(c, 0);
   double acc = 0.0;
   for (int i = tid; i < n; i += stride) {
     const int cc = __ldg(a.agg + i);
-    const double o = cc >= 0 ? fma(MG_GAMMA, g1[cc], (double)z[i]) : (double)z[i];
+    const float zi = z[i], fri = a.fr[i];
+    const double qi = q[i];
+    double o = (double)zi;
+    double w = (double)(float)qi - (double)fri;
+    if (cc >= 0) {
+      const double gc = g1[cc];
+      o = fma(MG_GAMMA, gc, o);
+      const double ap = ap_pairs(a.ragg, a.rval, __ldg(a.rcnt + i), i, n, g1, gc, __ldg(a.b.rs + i) * gc);
+      w = fma(MG_GAMMA, ap, w);
+    }
     out[i] = split2(o);
+    a.w[i] = w;
     acc += o;
   }
   write_partials(acc, 0.0, 1, slot, sh);
@@ -595,11 +814,14 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
   const double small = NONULL ? 1.0e-6 : 4.0;
   double red[2];
   double acc = 0.0;
-  auto precond = [&](const double* q, float2* out, double* slot) -> bool {
-    if (use_mg) return mg_vcycle_mixed(m, q, out, slot, sh, tid, stride);
+  // out = M^-1 (q - qshift), with q -= qshift stored back; block partial of sum(out) into slot
+  auto precond = [&](double* q, double qshift, float2* out, double* slot) -> bool {
+    if (use_mg) return mg_vcycle_mixed(m, q, qshift, out, slot, sh, tid, stride);
     double sum = 0.0;
     for (int i = tid; i < n; i += stride) {
-      const double o = NONULL ? q[i] * rinv1 : q[i] * a.rinvM[i];
+      const double qi = q[i] - qshift;
+      q[i] = qi;
+      const double o = NONULL ? qi * rinv1 : qi * a.rinvM[i];
       out[i] = split2(o);
       sum += o;
     }
@@ -642,27 +864,53 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
     if (rho == 0.0) { warn |= VEBI_WARN_BICGSTAB_BREAKDOWN; done = true; break; }
     const double beta = rho / (rho0 + 1.0e-15) * alpha / (omega + 1.0e-15);
     acc = 0.0;
-    for (int i = tid; i < n; i += stride) {
-      double pi = (iter == 1) ? a.r[i] : fma(beta, fma(-omega, a.v[i], a.p[i]), a.r[i]);
-      a.p[i] = pi;
-      acc += pi;
+    for (int i = tid; i < n; i += 2 * stride) {
+      const int j = i + stride;
+      const bool h = j < n;
+      const double ri = a.r[i], vi = a.v[i], pi = a.p[i];
+      const double rj = h ? a.r[j] : 0.0, vj = h ? a.v[j] : 0.0, pj = h ? a.p[j] : 0.0;
+      const double ni = (iter == 1) ? ri : fma(beta, fma(-omega, vi, pi), ri);
+      a.p[i] = ni;
+      acc += ni;
+      if (h) {
+        const double nj = (iter == 1) ? rj : fma(beta, fma(-omega, vj, pj), rj);
+        a.p[j] = nj;
+        acc += nj;
+      }
     }
+    double mean = 0.0;
     if (NONULL) {
       write_partials(acc, 0.0, 1, part, sh);
       if (!grid_sync(s)) return;
       reduce_partials(part, nb, 1, red, shv);
-      const double mean = red[0] / (double)n;
-      for (int i = tid; i < n; i += stride) a.p[i] = a.p[i] - mean;
+      mean = red[0] / (double)n;
     }
-    if (!precond(a.p, a.pi, part + 1 * (size_t)nb)) return;
+    if (!precond(a.p, mean, a.pi, part + 1 * (size_t)nb)) return;
     if (!grid_sync(s)) return;
     reduce_partials(part + 1 * (size_t)nb, nb, 1, red, shv);
     const double mp = NONULL ? red[0] / (double)n : 0.0;
     acc = 0.0;
-    for (int i = tid; i < n; i += stride) {
-      double vi = fma(-mp, __ldg(a.rs + i), spmv_diff32(a, a.pi, i));
-      a.v[i] = vi;
-      acc = fma(a.rb[i], vi, acc);
+    if (use_mg) {
+      for (int i = tid; i < n; i += 2 * stride) {
+        const int j = i + stride;
+        const bool h = j < n;
+        const double wi = m.w[i], rsi = __ldg(a.rs + i), rbi = a.rb[i];
+        const double wj = h ? m.w[j] : 0.0, rsj = h ? __ldg(a.rs + j) : 0.0, rbj = h ? a.rb[j] : 0.0;
+        const double vi = fma(-mp, rsi, wi);
+        a.v[i] = vi;
+        acc = fma(rbi, vi, acc);
+        if (h) {
+          const double vj = fma(-mp, rsj, wj);
+          a.v[j] = vj;
+          acc = fma(rbj, vj, acc);
+        }
+      }
+    } else {
+      for (int i = tid; i < n; i += stride) {
+        double vi = fma(-mp, __ldg(a.rs + i), spmv_diff32(a, a.pi, i));
+        a.v[i] = vi;
+        acc = fma(a.rb[i], vi, acc);
+      }
     }
     write_partials(acc, 0.0, 1, part + 2 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
@@ -670,11 +918,21 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
     alpha = rho / (red[0] + 1.0e-15);
     double a2 = 0.0;
     acc = 0.0;
-    for (int i = tid; i < n; i += stride) {
-      double si = fma(-alpha, a.v[i], a.r[i]);
+    for (int i = tid; i < n; i += 2 * stride) {
+      const int j = i + stride;
+      const bool h = j < n;
+      const double vi = a.v[i], ri = a.r[i];
+      const double vj = h ? a.v[j] : 0.0, rj = h ? a.r[j] : 0.0;
+      const double si = fma(-alpha, vi, ri);
       a.s[i] = si;
       acc = fma(si, si, acc);
       a2 += si;
+      if (h) {
+        const double sj = fma(-alpha, vj, rj);
+        a.s[j] = sj;
+        acc = fma(sj, sj, acc);
+        a2 += sj;
+      }
     }
     write_partials(acc, a2, 2, part + 4 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
@@ -688,19 +946,36 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
       done = true;
       break;
     }
-    if (NONULL)
-      for (int i = tid; i < n; i += stride) a.s[i] = a.s[i] - mean_s;
-    if (!precond(a.s, a.si, part + 3 * (size_t)nb)) return;
+    if (!precond(a.s, NONULL ? mean_s : 0.0, a.si, part + 3 * (size_t)nb)) return;
     if (!grid_sync(s)) return;
     reduce_partials(part + 3 * (size_t)nb, nb, 1, red, shv);
     const double ms = NONULL ? red[0] / (double)n : 0.0;
     acc = 0.0;
     a2 = 0.0;
-    for (int i = tid; i < n; i += stride) {
-      double ti = fma(-ms, __ldg(a.rs + i), spmv_diff32(a, a.si, i));
-      a.t[i] = ti;
-      acc = fma(ti, a.s[i], acc);
-      a2 = fma(ti, ti, a2);
+    if (use_mg) {
+      for (int i = tid; i < n; i += 2 * stride) {
+        const int j = i + stride;
+        const bool h = j < n;
+        const double wi = m.w[i], rsi = __ldg(a.rs + i), si = a.s[i];
+        const double wj = h ? m.w[j] : 0.0, rsj = h ? __ldg(a.rs + j) : 0.0, sj = h ? a.s[j] : 0.0;
+        const double ti = fma(-ms, rsi, wi);
+        a.t[i] = ti;
+        acc = fma(ti, si, acc);
+        a2 = fma(ti, ti, a2);
+        if (h) {
+          const double tj = fma(-ms, rsj, wj);
+          a.t[j] = tj;
+          acc = fma(tj, sj, acc);
+          a2 = fma(tj, tj, a2);
+        }
+      }
+    } else {
+      for (int i = tid; i < n; i += stride) {
+        double ti = fma(-ms, __ldg(a.rs + i), spmv_diff32(a, a.si, i));
+        a.t[i] = ti;
+        acc = fma(ti, a.s[i], acc);
+        a2 = fma(ti, ti, a2);
+      }
     }
     write_partials(acc, a2, 2, part + 6 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
@@ -708,12 +983,25 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
     omega = red[0] / (red[1] + 1.0e-15);
     acc = 0.0;
     a2 = 0.0;
-    for (int i = tid; i < n; i += stride) {
-      a.x[i] = fma(omega, join2(a.si[i]) - ms, fma(alpha, join2(a.pi[i]) - mp, a.x[i]));
-      double ri = fma(-omega, a.t[i], a.s[i]);
+    for (int i = tid; i < n; i += 2 * stride) {
+      const int j = i + stride;
+      const bool h = j < n;
+      const float2 sii = a.si[i], pii = a.pi[i];
+      const double xi = a.x[i], ti = a.t[i], s_i = a.s[i], rbi = a.rb[i];
+      const float2 sij = h ? a.si[j] : make_float2(0.f, 0.f), pij = h ? a.pi[j] : make_float2(0.f, 0.f);
+      const double xj = h ? a.x[j] : 0.0, tj = h ? a.t[j] : 0.0, s_j = h ? a.s[j] : 0.0, rbj = h ? a.rb[j] : 0.0;
+      a.x[i] = fma(omega, join2(sii) - ms, fma(alpha, join2(pii) - mp, xi));
+      const double ri = fma(-omega, ti, s_i);
       a.r[i] = ri;
       acc = fma(ri, ri, acc);
-      a2 = fma(a.rb[i], ri, a2);
+      a2 = fma(rbi, ri, a2);
+      if (h) {
+        a.x[j] = fma(omega, join2(sij) - ms, fma(alpha, join2(pij) - mp, xj));
+        const double rj = fma(-omega, tj, s_j);
+        a.r[j] = rj;
+        acc = fma(rj, rj, acc);
+        a2 = fma(rbj, rj, a2);
+      }
     }
     write_partials(acc, a2, 2, part + 8 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
@@ -771,9 +1059,10 @@ static int mg_setup(Ctx& x) {
   VEBI_LAUNCH(x, k_mg_level1, grid_for(x.mg[0].n), TPB, c, x.d, x.mg[0], x.mg_ragg, x.mg_rval, x.mg_rcnt);
   for (int l = 0; l + 1 < nl; ++l)
     VEBI_LAUNCH(x, k_mg_coarsen, grid_for(x.mg[l + 1].n), TPB, x.mg[l], x.mg[l + 1], x.d.s);
+  VEBI_LAUNCH(x, k_mg_coarse_inverse, 1, 32, x.mg[nl - 1], x.mg_kinv, x.mg_kinv_ok, c.open_domain == 0 ? 1 : 0);
   int tail = nl - 1;
   for (int l = 0; l < nl; ++l)
-    if (x.mg[l].n <= MG_BLOCK_ROWS) { tail = l; break; }
+    if (x.mg[l].n <= x.mg_block_rows) { tail = l; break; }
   return tail;
 }
 
@@ -798,7 +1087,8 @@ void launch_ppe_mg_mixed(Ctx& x) {
                     d.rowsum, d.ppe_val32, d.ppe_col, d.ij_count, d.s, (long long)c.npfb, c.npfb, c.itermax, c.tol,
                     c.warm_start},
              x.d_mg, (int)x.mg.size(), tail, d.cellpart, d.cell_start, d.cell_cnt, d.ip, (float*)x.mg_z,
-             (float*)x.mg_fr, (float*)x.mg_dinv0};
+             (float*)x.mg_fr, (float*)x.mg_dinv0, x.mg_ragg, x.mg_rcnt, x.mg_rval, x.mg_w, x.mg_kinv,
+             x.mg_kinv_ok};
   if (c.open_domain == 0) cudaLaunchKernelEx(&cfg, k_bicgstab_mixed_mg<true>, m);
   else cudaLaunchKernelEx(&cfg, k_bicgstab_mixed_mg<false>, m);
   x.launches++;
@@ -825,7 +1115,8 @@ void launch_ppe_mg(Ctx& x) {
   MgArgs m{BiArgs{d.bx, d.br, d.brb, d.bv, d.bp, d.bpi, d.bs, d.bsi, d.bt, d.bM, d.partials, d.p, d.ppe_B,
                   d.ppe_diag, d.ppe_val, d.ppe_col, d.ij_count, d.s, (long long)c.npfb, c.npfb, c.itermax, c.tol,
                   c.warm_start},
-           x.d_mg, nl, tail, d.cellpart, d.cell_start, d.cell_cnt, d.ip, x.mg_z, x.mg_fr, x.mg_dinv0, x.mg_rsum};
+           x.d_mg, nl, tail, d.cellpart, d.cell_start, d.cell_cnt, d.ip, x.mg_z, x.mg_fr, x.mg_dinv0, x.mg_rsum,
+           x.mg_ragg, x.mg_rcnt, x.mg_rval, x.mg_w, x.mg_kinv, x.mg_kinv_ok};
   if (c.open_domain == 0) cudaLaunchKernelEx(&cfg, k_bicgstab_mg<true>, m);
   else cudaLaunchKernelEx(&cfg, k_bicgstab_mg<false>, m);
   x.launches++;

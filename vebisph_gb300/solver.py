@@ -117,6 +117,9 @@ class StepSolver:
     def set_solver_grid(self, rows_per_thread: int):
         self._check(self.lib.vebi_set_solver_grid(self.h, int(rows_per_thread)), "vebi_set_solver_grid")
 
+    def set_coarse_block_rows(self, rows: int):
+        self._check(self.lib.vebi_set_coarse_block_rows(self.h, int(rows)), "vebi_set_coarse_block_rows")
+
     # -- output files (output.F90) ------------------------------------------------------
     def dump_async(self):
         """Snapshot the fields after the last step; the host copies overlap later steps."""
@@ -255,18 +258,30 @@ class BatchSolver:
         for inst in self.instances:
             inst.set_solver_grid(rows_per_thread)
 
-    def autotune(self, candidates=(1, 2, 4, 8)) -> dict:
-        """Pick the solver rows-per-thread of the batch by measurement: one step to capture the
-        graphs, one timed step per candidate (these are real steps of the simulations)."""
+    def set_coarse_block_rows(self, rows: int):
+        for inst in self.instances:
+            inst.set_coarse_block_rows(rows)
+
+    def autotune(self, candidates=(1, 2, 4, 8), coarse_candidates=(2048,)) -> dict:
+        """Pick the batch's solver tiles by measurement: the rows each solver thread owns (so
+        the rows per block and the blocks per instance) and, with the multigrid preconditioner,
+        the size up to which coarse levels run in one block.  Every pair of candidates costs one
+        step to capture the graphs and one timed step (real steps of the simulations).  The rows
+        per thread set the solver's block count and so the order of its block-partial sums
+        (results move by rounding); the coarse-level size leaves results unchanged."""
         times = {}
         for r in candidates:
-            self.set_solver_grid(r)
-            self.step(1)
-            ms, _ = self.step(1)
-            times[r] = ms
+            for cb in coarse_candidates:
+                self.set_solver_grid(r)
+                self.set_coarse_block_rows(cb)
+                self.step(1)
+                ms, _ = self.step(1)
+                times[(r, cb)] = ms
         best = min(times, key=times.get)
-        self.set_solver_grid(best)
-        return {"rows_per_thread": best, "ms_per_candidate": times}
+        self.set_solver_grid(best[0])
+        self.set_coarse_block_rows(best[1])
+        return {"rows_per_thread": best[0], "coarse_block_rows": best[1],
+                "ms_per_candidate": {f"{r},{cb}": v for (r, cb), v in times.items()}}
 
     def close(self):
         if getattr(self, "h", None):
