@@ -530,6 +530,10 @@ def run_batch(args, dist: Dist):
     bprec = abi.PREC_MIXED if args.batch_precision == "mixed" else abi.PREC_FP64
     b = BatchSolver(cl, precision=bprec)
     t_create = time.perf_counter() - t0
+    # divergence guard: each instance fails with its own status if its velocity turns non-finite
+    # or passes 100x its flow's velocity scale (the channels and cylinders are scaled to ~1)
+    for inst, c in zip(b.instances, cl):
+        inst.set_velocity_limit(100.0 * max(1.0, float(np.abs(c.u).max())))
     tune = b.autotune(candidates=tuple(int(v) for v in args.tune.split(",")),
                       coarse_candidates=(tuple(int(v) for v in args.tune_coarse.split(",")) if mg else (2048,)))
     done = 2 * len(tune["ms_per_candidate"])

@@ -236,19 +236,19 @@ __global__ void __launch_bounds__(TPB) k_neighbours(Consts c, Dev d) {
         for (int u = 0; u < NB_UNROLL; ++u) {
           const float f1 = ax - pv[u].x, f2 = ay - pv[u].y;
           const float qq = fmaf(f1, f1, f2 * f2);
-          if (qq <= hi) {
-            const int j = __float_as_int(pv[u].z);
-            bool take = qq < lo && qq > band;
-            if (!take) {  // near a threshold: the reference's FP64 test
-              const double r1 = xi - d.rx[j], r2 = yi - d.ry[j];
-              const double rr2 = r1 * r1 + r2 * r2;
-              take = rr2 > 0.0 && rr2 <= c.sup_size_2;
-            }
-            if (take) {
-              if (cnt < c.nplink) out[(size_t)cnt * c.npfb] = j;
-              else over = true;
-              ++cnt;
-            }
+          const int j = __float_as_int(pv[u].z);
+          // decided in FP32 far from both thresholds; the branch below is taken only inside
+          // the bands (and for the particle itself), so the common path does not diverge
+          bool take = (qq < lo) & (qq > band);
+          if ((qq <= hi) & !take) {  // near a threshold: the reference's FP64 test
+            const double r1 = xi - d.rx[j], r2 = yi - d.ry[j];
+            const double rr2 = r1 * r1 + r2 * r2;
+            take = rr2 > 0.0 && rr2 <= c.sup_size_2;
+          }
+          if (take) {
+            if (cnt < c.nplink) out[(size_t)cnt * c.npfb] = j;
+            else over = true;
+            ++cnt;
           }
         }
       }

@@ -231,12 +231,12 @@ __global__ void __launch_bounds__(32) k_mg_coarse_inverse(MgLevel K, double* inv
   if (r == 0) *ok = good ? 1 : 0;
 }
 
-// sum over a row's cell pairs t = 1..m-1 of (A P)_ic (g_c - g_own), in pair order.  The pairs
-// are taken four at a time with all their loads issued before the gathers of g they index,
-// so a row costs one or two dependent round trips instead of two per pair.
+// sum over a row's cell pairs t = t_first..m-1 of (A P)_ic (g_c - g_own), in pair order,
+// four pairs at a time with all their loads issued before the gathers of g they index
 __device__ __forceinline__ double ap_pairs(const int* __restrict__ ragg, const double* __restrict__ rval, int m,
-                                           size_t i, size_t n, const double* g, double gc, double ap) {
-  for (int t0 = 1; t0 < m; t0 += 4) {
+                                           size_t i, size_t n, const double* g, double gc, double ap,
+                                           int t_first = 1) {
+  for (int t0 = t_first; t0 < m; t0 += 4) {
     int c4[4];
     double v4[4];
 #pragma unroll
@@ -253,6 +253,43 @@ __device__ __forceinline__ double ap_pairs(const int* __restrict__ ragg, const d
     for (int u = 0; u < 4; ++u)
       if (c4[u] >= 0) ap = fma(v4[u], g4[u] - gc, ap);
   }
+  return ap;
+}
+
+// The first four pairs beyond the row's own cell, loaded without waiting for the row's pair
+// count: the pair table has MG_ROW_SLOTS slots for every row, so slots past the count are in
+// bounds; they are masked once the count is known.  Most rows have at most five pairs, so the
+// row's loads form one round trip and the gathers of g a second.
+struct ApHead {
+  int c[4];
+  double v[4];
+};
+
+__device__ __forceinline__ ApHead ap_head(const int* __restrict__ ragg, const double* __restrict__ rval, size_t i,
+                                          size_t n) {
+  ApHead h;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    h.c[u] = __ldg(ragg + (size_t)(1 + u) * n + i);
+    h.v[u] = __ldg(rval + (size_t)(1 + u) * n + i);
+  }
+  return h;
+}
+
+// rowsum_i g_own + sum_c (A P)_ic (g_c - g_own) from a prefetched head and the row's count m;
+// own = the row's cell, whose value g[own] = gc.  Masked slots gather g[own]: an index read
+// past the row's count is never used as an address.
+__device__ __forceinline__ double ap_row(const ApHead& h, const int* __restrict__ ragg,
+                                         const double* __restrict__ rval, int m, size_t i, size_t n,
+                                         const double* g, int own, double gc, double rs) {
+  double g4[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) g4[u] = g[1 + u < m ? h.c[u] : own];
+  double ap = rs * gc;
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+    if (1 + u < m) ap = fma(h.v[u], g4[u] - gc, ap);
+  if (m > 5) ap = ap_pairs(ragg, rval, m, i, n, g, gc, ap, 5);
   return ap;
 }
 
@@ -413,15 +450,15 @@ __device__ bool mg_vcycle(const MgArgs& a, double* q, double qshift, double* out
   const double* g1 = lv_sol(a, 0);
   double acc = 0.0;
   for (int i = tid; i < n; i += stride) {
-    const int c = __ldg(a.agg + i);
-    const double zi = z[i], qi = q[i], fri = a.fr[i];
+    const int c = __ldg(a.agg + i), mc = __ldg(a.rcnt + i);
+    const double zi = z[i], qi = q[i], fri = a.fr[i], rsi = a.rsum[i];
+    const ApHead hd = ap_head(a.ragg, a.rval, i, n);
     double o = zi;
     double w = qi - fri;
     if (c >= 0) {
       const double gc = g1[c];
       o = fma(MG_GAMMA, gc, o);
-      const double ap = ap_pairs(a.ragg, a.rval, __ldg(a.rcnt + i), i, n, g1, gc, a.rsum[i] * gc);
-      w = fma(MG_GAMMA, ap, w);
+      w = fma(MG_GAMMA, ap_row(hd, a.ragg, a.rval, mc, i, n, g1, c, gc, rsi), w);
     }
     out[i] = o;
     a.w[i] = w;
@@ -778,16 +815,16 @@ __device__ bool mg_vcycle_mixed(const MgMxArgs& a, double* q, double qshift, flo
   const double* g1 = lv_sol(c, 0);
   double acc = 0.0;
   for (int i = tid; i < n; i += stride) {
-    const int cc = __ldg(a.agg + i);
+    const int cc = __ldg(a.agg + i), mc = __ldg(a.rcnt + i);
     const float zi = z[i], fri = a.fr[i];
-    const double qi = q[i];
+    const double qi = q[i], rsi = __ldg(a.b.rs + i);
+    const ApHead hd = ap_head(a.ragg, a.rval, i, n);
     double o = (double)zi;
     double w = (double)(float)qi - (double)fri;
     if (cc >= 0) {
       const double gc = g1[cc];
       o = fma(MG_GAMMA, gc, o);
-      const double ap = ap_pairs(a.ragg, a.rval, __ldg(a.rcnt + i), i, n, g1, gc, __ldg(a.b.rs + i) * gc);
-      w = fma(MG_GAMMA, ap, w);
+      w = fma(MG_GAMMA, ap_row(hd, a.ragg, a.rval, mc, i, n, g1, cc, gc, rsi), w);
     }
     out[i] = split2(o);
     a.w[i] = w;
