@@ -176,10 +176,12 @@ __global__ void k_cell_offsets(Consts c, Dev d) {
 // Pair list, 0 < r^2 <= 9h^2, cells in the reference's order C, E, NE, SE, W, NW, SW, N, S
 // (neighbour_finding_mod.F90:261-365), each cell's candidates in its list order.
 //
-// One thread per cell-list position, so a warp holds the particles of two or three adjacent
-// cells and its lanes walk the same candidate lists: every candidate load is a near-broadcast
-// of the cell-ordered record (pko: offsets and particle index in one 16-byte load).  Each
-// list is written to its particle's own column, ij_link[k][i].
+// One thread per particle in index order, so the lanes' stores of slot k of ij_link[k][i] fall
+// on consecutive columns.  Candidates come from the cell-ordered record (pko: FP32 offsets and
+// particle index in one 16-byte load): lanes in the same cell read the same record, and no
+// load depends on another.  (Lanes in cell-list order instead make the loads near-broadcasts
+// but scatter the stores; measured at 4M: 1.34 ms against 0.93 ms for index order with
+// separate index and offset gathers.)
 //
 // The test is decided in FP32 when it is far from both thresholds, and in FP64 on the
 // reference's expression otherwise.  Error bound of the FP32 r^2: the offsets are < S (the
@@ -192,13 +194,12 @@ __global__ void k_cell_offsets(Consts c, Dev d) {
 constexpr int NB_UNROLL = 4;
 
 __global__ void __launch_bounds__(TPB) k_neighbours(Consts c, Dev d) {
-  const int tot = d.cell_start[c.nct];
-  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool mine = i < c.npfb;  // every lane stays to the warp reduction at the end
   int cnt = 0;
-  const int i = pos < tot ? d.ip[pos] : c.npfb;
-  if (i < c.npfb) {
+  if (mine && !d.inbin[i] && d.cellpart[i] >= 0) {
     const double xi = d.rx[i], yi = d.ry[i];
-    const float4 po = d.pko[pos];
+    const float4 po = d.pk[i];
     const float S = (float)c.cell_size;
     const float S2 = (float)c.sup_size_2;
     const float band = 64.0f * 5.9604645e-8f * S2;
@@ -257,8 +258,8 @@ __global__ void __launch_bounds__(TPB) k_neighbours(Consts c, Dev d) {
       set_error(d.s, VEBI_ERR_NEIGH_CAPACITY);
       cnt = c.nplink;
     }
-    d.ij_count[i] = cnt;
   }
+  if (mine) d.ij_count[i] = cnt;
   // one atomic per warp for the population maximum
   for (int o = 16; o > 0; o >>= 1) cnt = max(cnt, __shfl_xor_sync(0xffffffffu, cnt, o));
   if ((threadIdx.x & 31) == 0 && cnt > 0) atomicMax(&d.s->maxneigh, cnt);
@@ -276,9 +277,7 @@ void launch_cells_neighbours(Ctx& x) {
   VEBI_LAUNCH(x, k_cell_sort, grid_for((long long)c.nct * 32), TPB, c, x.d);
   VEBI_LAUNCH(x, k_cell_offsets, x.gs_blocks, TPB, c, x.d);
   stage_mark(x, 3);
-  // particles outside the cells (in the bin) keep an empty list
-  cudaMemsetAsync(x.d.ij_count, 0, sizeof(int) * (size_t)c.npfb, x.st);
-  VEBI_LAUNCH(x, k_neighbours, grid_for(c.cap), TPB, c, x.d);
+  VEBI_LAUNCH(x, k_neighbours, grid_for(c.npfb), TPB, c, x.d);
 }
 
 }  // namespace vebi

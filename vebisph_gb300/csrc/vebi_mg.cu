@@ -814,21 +814,36 @@ __device__ bool mg_vcycle_mixed(const MgMxArgs& a, double* q, double qshift, flo
   // gamma (A P) g1 in difference form with the mixed operator's row sums
   const double* g1 = lv_sol(c, 0);
   double acc = 0.0;
-  for (int i = tid; i < n; i += stride) {
-    const int cc = __ldg(a.agg + i), mc = __ldg(a.rcnt + i);
-    const float zi = z[i], fri = a.fr[i];
-    const double qi = q[i], rsi = __ldg(a.b.rs + i);
-    const ApHead hd = ap_head(a.ragg, a.rval, i, n);
-    double o = (double)zi;
-    double w = (double)(float)qi - (double)fri;
-    if (cc >= 0) {
-      const double gc = g1[cc];
-      o = fma(MG_GAMMA, gc, o);
-      w = fma(MG_GAMMA, ap_row(hd, a.ragg, a.rval, mc, i, n, g1, cc, gc, rsi), w);
+  // two rows per pass (i and i + stride), every load of both issued before the gathers
+  for (int i = tid; i < n; i += 2 * stride) {
+    const int j = i + stride;
+    const bool h = j < n;
+    const int jj = h ? j : i;  // a second row past n repeats row i's loads and stores nothing
+    const int cci = __ldg(a.agg + i), mci = __ldg(a.rcnt + i);
+    const int ccj = __ldg(a.agg + jj), mcj = __ldg(a.rcnt + jj);
+    const float zi = z[i], fri = a.fr[i], zj = z[jj], frj = a.fr[jj];
+    const double qi = q[i], rsi = __ldg(a.b.rs + i), qj = q[jj], rsj = __ldg(a.b.rs + jj);
+    const ApHead hi_ = ap_head(a.ragg, a.rval, i, n);
+    const ApHead hj_ = ap_head(a.ragg, a.rval, jj, n);
+    const double gci = g1[cci >= 0 ? cci : 0], gcj = g1[ccj >= 0 ? ccj : 0];
+    double oi = (double)zi, wi = (double)(float)qi - (double)fri;
+    double oj = (double)zj, wj = (double)(float)qj - (double)frj;
+    if (cci >= 0) {
+      oi = fma(MG_GAMMA, gci, oi);
+      wi = fma(MG_GAMMA, ap_row(hi_, a.ragg, a.rval, mci, i, n, g1, cci, gci, rsi), wi);
     }
-    out[i] = split2(o);
-    a.w[i] = w;
-    acc += o;
+    if (ccj >= 0) {
+      oj = fma(MG_GAMMA, gcj, oj);
+      wj = fma(MG_GAMMA, ap_row(hj_, a.ragg, a.rval, mcj, jj, n, g1, ccj, gcj, rsj), wj);
+    }
+    out[i] = split2(oi);
+    a.w[i] = wi;
+    acc += oi;
+    if (h) {
+      out[j] = split2(oj);
+      a.w[j] = wj;
+      acc += oj;
+    }
   }
   write_partials(acc, 0.0, 1, slot, sh);
   return true;
