@@ -207,24 +207,28 @@ def stage_bandwidth(stage_ms_per_step: dict, n: int, kbar: float, mixed: bool, p
 
 def mg_bytes_per_iteration(n_rows: int, nnz_off: int, n_cells: int, mixed: bool = False,
                            pairs: float = 5.0) -> float:
-    """Algorithmic bytes of one multigrid-preconditioned BiCGSTAB iteration (closed domain).
+    """Algorithmic bytes of one multigrid-preconditioned BiCGSTAB iteration (closed domain),
+    pass by pass; k = off-diagonal slots per row, p = (cell, value) pairs of A P per row.
 
-    BiCGSTAB vector phases: FP64 168 B per row (p update 32, mean removal 24, s 24, s mean
-    removal 24, x/r update 64), mixed 184 (the same with FP32 (hi, lo) splits of the
-    preconditioned directions); the two products A M^-1 p and A M^-1 s are not separate sparse
-    products: the V-cycle returns w = A M^-1 q, so each costs a pass reading w, the row sum and
-    the dot operand and writing the product, 32 B per row.
-    Two V-cycles.  Particle level (pre-smoothing only): FP64 12 B per slot + 100 B per row (the
-    first sweep 24, the residual product 44, restriction 12, prolongation and output 20), mixed
-    8 B per slot + 72 B per row (16, 32, 8, 16); then w = (q - fr) + gamma (A P) g: q, fr, the
-    row sum, the pair count and w (FP64 36 B, mixed 32 B) plus 12 B per (cell, value) pair of the
-    row beyond its own cell (`pairs` = mean pairs per row).  Coarse levels: ~390 B per cell (the
-    cell level's ELL rows read by the residual and the smoothing sweep, work vectors, and the
-    geometric sum of the coarser levels)."""
-    outer = 2.0 * 32.0 * n_rows + (184.0 if mixed else 168.0) * n_rows
-    fine = (8.0 * nnz_off + 72.0 * n_rows) if mixed else (12.0 * nnz_off + 100.0 * n_rows)
-    fine += ((32.0 if mixed else 36.0) + 12.0 * max(pairs - 1.0, 0.0)) * n_rows
-    return outer + 2.0 * (fine + 390.0 * n_cells)
+    BiCGSTAB passes, 184 B per row in both precisions: p update 32 (r, v, p; p), v 32 (w, row
+    sum, r_bar; v), s 24 (v, r; s), t 32 (w, row sum, s; t), x/r update 64 (the two
+    preconditioned directions, x, t, s, r_bar; x, r -- the directions are FP64 or FP32 (hi, lo)
+    pairs, 8 B either way).  The products A M^-1 p and A M^-1 s are the V-cycle's w.
+    Two V-cycles, particle level:
+      mean removal and first sweep: FP64 32 B (q, 1/diag; q, z), mixed 24 (FP32 1/diag and z);
+      residual: FP64 36 + 12k (count, diagonal, z_i, q; fr), mixed 28 + 8k (count, row sum,
+        FP32 z_i, q; FP32 fr);
+      restriction: FP64 12, mixed 8 (cell list entry, fr);
+      output: FP64 56, mixed 48 (cell, pair count, z, fr, q, row sum; the direction and w) plus
+        12 B per pair beyond the row's own cell.
+    Coarse levels: ~390 B per cell (the cell level's ELL rows read by the residual and the
+    smoothing sweep, work vectors, and the geometric sum of the coarser levels)."""
+    extra_pairs = 12.0 * max(pairs - 1.0, 0.0) * n_rows
+    if mixed:
+        fine = 8.0 * nnz_off + (24.0 + 28.0 + 8.0 + 48.0) * n_rows + extra_pairs
+    else:
+        fine = 12.0 * nnz_off + (32.0 + 36.0 + 12.0 + 56.0) * n_rows + extra_pairs
+    return 184.0 * n_rows + 2.0 * (fine + 390.0 * n_cells)
 
 
 def cpu_baseline(case, gpu_iters_per_step: float, itermax_sample: int):
@@ -320,6 +324,7 @@ def run_gb300(args, dist: Dist):
             "kernel": kname,
             "peak_kind": f"{peak_kind} hbm_gbs (burst copy)",
             "bytes_per_iteration": bytes_iter, "iterations_per_launch": iters_per_step,
+            "mg_pairs_per_row": round(pairs, 3) if mg else None,
             "launch_ms": round(per_launch_s * 1e3, 3)}
     # end to end through the C-ABI with host buffers (pinned), copies inside the timed region:
     # the time loop of a host driver that owns the state in its arrays (the Fortran module
@@ -500,7 +505,10 @@ def run_adjoint(args, dist: Dist, ref: dict | None = None) -> dict:
             "forward_ms_per_step": 1e3 * t_fwd / N, "record_ms_per_step": 1e3 * t_rec / N,
             "reverse_ms_per_step": 1e3 * t_rev / N, "adjoint_over_forward": t_rev / t_fwd,
             "forward_LS_iters_per_step": fwd_iters / N, "transposed_LS_iters_per_step": g["ls_iters"] / N,
+            "near_pole_particles_per_step": sf["n_near_pole_total"] / N,
             "dJ_dWi": g["wi"], "grad_theta_max_abs": float(np.abs(g["theta"]).max()),
+            "grad_theta_abs_percentiles": {str(q): float(np.percentile(np.abs(g["theta"][nbS:]), q))
+                                           for q in (50, 99, 99.99, 100)},
             "directional_derivatives": dirs,
             "finite_differences": fd,
             "fd_eps": eps if fd else None,
@@ -822,7 +830,7 @@ def main():
     ap.add_argument("--adjoint-tol", type=float, default=1.0e-8, help="PPE tolerance of the adjoint workload")
     ap.add_argument("--adjoint-spinup", type=int, default=20, help="steps run before the adjoint window")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement of the default line")
-    ap.add_argument("--default-adjoint-fd", type=int, default=4,
+    ap.add_argument("--default-adjoint-fd", type=int, default=2,
                     help="central-difference directions of the default line's adjoint (each replays the window twice)")
     ap.add_argument("--adjoint-precision", default="fp64", choices=["fp64", "mixed"],
                     help="arithmetic of the adjoint workload's forward step")
@@ -886,6 +894,10 @@ def main():
             res["adjoint"] = run_adjoint(aargs, dist)
             aargs.adjoint_precision, aargs.adjoint_fd = "mixed", 0
             res["adjoint_mixed"] = run_adjoint(aargs, dist, ref=res["adjoint"])
+            # the same window, Newtonian: the log-conformation update's eigenvalue-gap pole
+            # (predictor_mod.F90:213) is absent, so central differences can follow the adjoint
+            aargs.adjoint_precision, aargs.adjoint_fd, aargs.adjoint_const_mod = "fp64", args.default_adjoint_fd, 1
+            res["adjoint_newtonian"] = run_adjoint(aargs, dist)
         res.pop("_fields", None)
     else:
         from oracle import build as ob

@@ -144,6 +144,10 @@ typedef struct vebi_step_stats {
   int32_t refine_iters; /* mixed precision: outer refinement sweeps                  */
   int32_t LS_iters_total; /* vebi_run_steps: BiCGSTAB iterations summed over the steps */
   int32_t nsteps;       /* steps these statistics cover                              */
+  int32_t n_near_pole;  /* diagnostic (no reference counterpart): particles whose conformation
+                           eigenvalues are < 1e-7 apart, near the 1/(L2 - L1 + 1e-10) pole of the
+                           log-conformation update (predictor_mod.F90:213) */
+  int32_t n_near_pole_total; /* vebi_run_steps: the same summed over the steps             */
 } vebi_step_stats;
 
 typedef struct vebi_ctx vebi_ctx;

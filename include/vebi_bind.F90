@@ -40,6 +40,7 @@ module vebi_bind
      real(c_double) :: stage_ms(16), circle_force(2)
      integer(c_int32_t) :: LS_iters, n_inbin, np, npfb, nmirror, maxneighbours, n_escapees
      integer(c_int32_t) :: error, warnings, gpu_launches, refine_iters, LS_iters_total, nsteps
+     integer(c_int32_t) :: n_near_pole, n_near_pole_total
   end type vebi_step_stats
 
   type, bind(C) :: vebi_dump_info

@@ -85,6 +85,7 @@ class VebiStepStats(C.Structure):
         ("n_escapees", C.c_int32), ("error", C.c_int32), ("warnings", C.c_int32),
         ("gpu_launches", C.c_int32), ("refine_iters", C.c_int32),
         ("LS_iters_total", C.c_int32), ("nsteps", C.c_int32),
+        ("n_near_pole", C.c_int32), ("n_near_pole_total", C.c_int32),
     ]
 
     def as_dict(self) -> dict:

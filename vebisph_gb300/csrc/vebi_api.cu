@@ -397,6 +397,8 @@ static int finish_step(Ctx& x, vebi_step_stats* stats, bool sync) {
   o.gpu_launches = x.launches;
   o.refine_iters = s.refine_iters;
   o.LS_iters_total = s.ls_iters_total;
+  o.n_near_pole = s.n_near_pole;
+  o.n_near_pole_total = s.n_near_pole_total;
   o.nsteps = 1;
   if (x.timing && sync) {
     int prev = -1;
@@ -521,6 +523,7 @@ int vebi_run_steps(vebi_ctx* h, double x_mint, double y_mint, double x_maxt, dou
   double acc[VEBI_NSTAGES] = {};
   x.launches = 0;
   cudaMemsetAsync(&x.d.s->ls_iters_total, 0, sizeof(int), x.st);
+  cudaMemsetAsync(&x.d.s->n_near_pole_total, 0, sizeof(int), x.st);
   cudaEventRecord(e0, x.st);
   for (int s = 0; s < nsteps; ++s) {
     launch_step(x, 0);

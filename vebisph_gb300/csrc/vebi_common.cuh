@@ -79,6 +79,8 @@ struct Scal {
   int ls_iters_total;                // summed over the steps of one vebi_run_steps call
   int first_error;                   // first failing status since the last upload (sticky)
   int mg_fail;                       // multigrid set-up overflowed a coarse row: solve without it
+  int n_near_pole;                   // particles whose conformation eigenvalues are < 1e-7 apart
+  int n_near_pole_total;             // the same summed over the steps of one vebi_run_steps call
 };
 
 // multigrid preconditioner (opt-in): coarse-row capacity, coarsest size, level cap, levels run

@@ -42,6 +42,7 @@ __global__ void k_step_reset(Scal* s, int npfb, int nbS) {
   s->bar_count = 0;
   s->refine_iters = 0;
   s->mg_fail = 0;
+  s->n_near_pole = 0;
 }
 
 // STEP 1-2: keep r0,u0 and reduce max|u| over the fluid (set_time_step)

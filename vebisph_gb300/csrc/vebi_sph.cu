@@ -254,6 +254,14 @@ __global__ void k_logconf(Consts c, Dev d) {
   double L1, L2;
   M2 R;
   calc_eigens(A, L1, L2, R);
+  {  // diagnostic: particles within reach of the 1/(L2 - L1 + 1e-10) pole of step 5
+    const unsigned am = __activemask();
+    const unsigned near = __ballot_sync(am, fabs(L2 - L1) < 1.0e-7);
+    if ((threadIdx.x & 31) == __ffs(am) - 1 && near) {
+      atomicAdd(&d.s->n_near_pole, __popc(near));
+      atomicAdd(&d.s->n_near_pole_total, __popc(near));
+    }
+  }
   // step 3: Psi = R log(Lambda) R^T
   M2 D{log(L1), 0.0, 0.0, log(L2)};
   M2 Psi0 = mm(R, mm(D, tr(R)));
