@@ -562,7 +562,8 @@ def run_batch(args, dist: Dist):
     value = dist.sum(float(n_live * args.steps)) / (t_max * 1e-3)
     # the same instances one by one, plain FP64, timed over the same K steps (device events)
     serial_ms, serial_units, du, dp, per, spread = 0.0, 0, [], [], [], []
-    for i, (c, fm) in enumerate(zip(cl, fields)):
+    light = getattr(args, "batch_light", False)  # the default line: speed only, no accuracy reruns
+    for i, (c, fm) in enumerate(zip([] if light else cl, fields)):
         s1 = StepSolver(c, precision=abi.PREC_FP64)
         rec = {"i": i, "case": c.name, "n_fluid": c.n_fluid, "El": c.El, "beta": c.beta,
                "batch_error": failed.get(i, 0), "LS_iters_batch": iters[i]}
@@ -603,7 +604,7 @@ def run_batch(args, dist: Dist):
             rec["fp64_error"] = e.status
         s1.close()
         per.append(rec)
-    serial_value = serial_units / (serial_ms * 1e-3)
+    serial_value = serial_units / (serial_ms * 1e-3) if serial_ms > 0 else None
     plain = None
     if mg:  # the reference's solver one by one: K steps from the initial state (speed only)
         pms, punits = 0.0, 0
@@ -642,10 +643,10 @@ def run_batch(args, dist: Dist):
         "failed_instances": {"batch": len(failed), "serial_fp64": sum(1 for r in per if "fp64_error" in r),
                              "both": sum(1 for r in per if "fp64_error" in r and r["batch_error"]),
                              "statuses": sorted(set(failed.values()))},
-        "serial_fp64": {"value": serial_value, "unit": UNIT, "ms_per_step": serial_ms / args.steps,
-                        "speedup_of_batch": value / serial_value, "counted": "instances that did not fail",
-                        "path": "one StepSolver per instance, FP64, same PPE preconditioner as the batch, "
-                                "graph-replayed steps, summed device time"},
+        "serial_fp64": ({"value": serial_value, "unit": UNIT, "ms_per_step": serial_ms / args.steps,
+                         "speedup_of_batch": value / serial_value, "counted": "instances that did not fail",
+                         "path": "one StepSolver per instance, FP64, same PPE preconditioner as the batch, "
+                                 "graph-replayed steps, summed device time"} if serial_value else None),
         "serial_plain_fp64": plain,
         "speedup_vs_serial_plain_fp64": (value / plain["value"]) if plain else None,
         "batch_vs_serial_fp64": ({
@@ -653,7 +654,7 @@ def run_batch(args, dist: Dist):
             "u_rel_median": float(np.median(du)), "u_rel_p90": float(np.percentile(du, 90)),
             "u_within_1e-4": int((du <= 1e-4).sum()), "u_within_1e-3": int((du <= 1e-3).sum()),
             "u_within_1e-2": int((du <= 1e-2).sum()), "p_rel_median": float(np.median(dp)),
-            "fp64_spread_median": float(np.median(spread)),
+            "fp64_spread_median": float(np.median(spread[np.isfinite(spread)])) if np.isfinite(spread).any() else None,
             "u_within_max_1e-4_2x_fp64_spread": int((du <= np.maximum(1e-4, 2.0 * spread)).sum()),
             "spread_note": "fp64_spread: FP64 rerun from velocities perturbed by 6e-8 relative (FP32 rounding) "
                            "after the same steps; the flow's own amplification of rounding-level differences"}
@@ -830,6 +831,7 @@ def main():
     ap.add_argument("--adjoint-tol", type=float, default=1.0e-8, help="PPE tolerance of the adjoint workload")
     ap.add_argument("--adjoint-spinup", type=int, default=20, help="steps run before the adjoint window")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement of the default line")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched sweep of the default line")
     ap.add_argument("--default-adjoint-fd", type=int, default=2,
                     help="central-difference directions of the default line's adjoint (each replays the window twice)")
     ap.add_argument("--adjoint-precision", default="fp64", choices=["fp64", "mixed"],
@@ -841,8 +843,9 @@ def main():
         args.warmup = 3
     if args.e2e_steps <= 0:
         args.e2e_steps = args.steps
-    if args.batch:
-        # independent instances run as concurrent graph branches: more hardware queues
+    if args.batch or (args.impl == "gb300" and not args.no_batch):
+        # independent instances run as concurrent graph branches: more hardware queues (set
+        # before the first CUDA call of the process)
         os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     dist = Dist()
     if args.impl == "gb300":
@@ -898,6 +901,16 @@ def main():
             # (predictor_mod.F90:213) is absent, so central differences can follow the adjoint
             aargs.adjoint_precision, aargs.adjoint_fd, aargs.adjoint_const_mod = "fp64", args.default_adjoint_fd, 1
             res["adjoint_newtonian"] = run_adjoint(aargs, dist)
+        if not args.no_batch and not args.batch and dist.world == 1:
+            # the batched sweep (512 instances, mixed + multigrid, autotuned tiles) against the same
+            # instances run one by one with the plain FP64 step; speed only (the accuracy
+            # comparison is `bench.py --batch 512`)
+            bargs = argparse.Namespace(**vars(args))
+            bargs.batch, bargs.batch_light, bargs.steps, bargs.warmup = 512, True, 3, 3
+            b = run_batch(bargs, dist)
+            res["batch"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "config", "LS_iters_per_step",
+                                              "failed_instances", "serial_plain_fp64",
+                                              "speedup_vs_serial_plain_fp64", "gpu_launches", "clocks")}
         res.pop("_fields", None)
     else:
         from oracle import build as ob
