@@ -39,15 +39,20 @@ def _stale(out: pathlib.Path, deps) -> bool:
     return any(p.stat().st_mtime > t for p in deps)
 
 
-def build(force: bool = False, verbose: bool = False, extra: list | None = None) -> pathlib.Path:
-    OUT_DIR.mkdir(parents=True, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, extra: list | None = None,
+          out_dir: pathlib.Path | None = None) -> pathlib.Path:
+    """Compile the library into out_dir (default vebisph_gb300/_build); `extra` nvcc flags build
+    a variant (e.g. a diagnostic -D flag) that should go to its own out_dir."""
+    out = pathlib.Path(out_dir) if out_dir else OUT_DIR
+    lib = out / LIB.name
+    out.mkdir(parents=True, exist_ok=True)
     headers = list(CSRC.glob("*.cuh")) + [INCLUDE / "vebi.h"]
     nvcc = _nvcc()
     extra = extra or []
     objs = []
     jobs = []
     for src in sources():
-        obj = OUT_DIR / (src.stem + ".o")
+        obj = out / (src.stem + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
             jobs.append([nvcc, *ARCH, *NVFLAGS, *extra, "-c", str(src), "-o", str(obj)])
@@ -61,12 +66,12 @@ def build(force: bool = False, verbose: bool = False, extra: list | None = None)
                     print(r.stdout + r.stderr)
                 if r.returncode:
                     raise RuntimeError(f"nvcc failed on {j[-3]}")
-    if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs)]
+    if force or jobs or _stale(lib, objs):
+        cmd = [nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, objs)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode:
             raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":

@@ -1175,3 +1175,17 @@ void launch_ppe_mg(Ctx& x) {
 }
 
 }  // namespace vebi
+
+#ifdef VEBI_BARRIER_TIMESTAMPS
+// diagnostic build only: the multigrid solvers' barrier timestamps (see vebi_solver.cuh)
+extern "C" int vebi_barrier_timestamps_reset(void) {
+  unsigned int z = 0;
+  return (int)cudaMemcpyToSymbol(vebi::g_bar_n, &z, sizeof(z));
+}
+extern "C" int vebi_barrier_timestamps_read(unsigned long long* ts, unsigned int* n) {
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpyFromSymbol(n, vebi::g_bar_n, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMemcpyFromSymbol(ts, vebi::g_bar_ts, sizeof(unsigned long long) * 2 * vebi::BAR_TS_MAX);
+  return (int)e;
+}
+#endif

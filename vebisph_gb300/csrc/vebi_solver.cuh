@@ -8,10 +8,28 @@ namespace vebi {
 
 constexpr unsigned long long SPIN_LIMIT = 1ull << 25;  // ~2-4 s of __nanosleep(64) polls
 
+#ifdef VEBI_BARRIER_TIMESTAMPS
+// Diagnostic build only (vebisph_gb300/barrier_profile.py): block 0 records the global timer
+// when it arrives at and leaves every grid barrier, so the time of each solver phase and of the
+// wait for the slowest block can be read back.  Each translation unit has its own copy; the
+// solvers of vebi_mg.cu export theirs.
+constexpr int BAR_TS_MAX = 16384;
+static __device__ unsigned long long g_bar_ts[2][BAR_TS_MAX];
+static __device__ unsigned int g_bar_n;
+__device__ __forceinline__ unsigned long long bar_clock() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+#endif
+
 // bounded grid-wide barrier for a co-resident (cooperative) grid; false on error/timeout.
 // A block that polls more than `limit` times records VEBI_ERR_TIMEOUT and returns false, and so
 // does every block that arrives or polls after the error is recorded.
 __device__ __forceinline__ bool grid_sync_bounded(Scal* s, unsigned long long limit) {
+#ifdef VEBI_BARRIER_TIMESTAMPS
+  const unsigned long long ts_arrive = bar_clock();
+#endif
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile unsigned int* vgen = &s->bar_gen;
@@ -37,6 +55,15 @@ __device__ __forceinline__ bool grid_sync_bounded(Scal* s, unsigned long long li
     __threadfence();
   }
   __syncthreads();
+#ifdef VEBI_BARRIER_TIMESTAMPS
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const unsigned int q = g_bar_n++;
+    if (q < BAR_TS_MAX) {
+      g_bar_ts[0][q] = ts_arrive;
+      g_bar_ts[1][q] = bar_clock();
+    }
+  }
+#endif
   return *((volatile int*)&s->error) == 0;
 }
 
