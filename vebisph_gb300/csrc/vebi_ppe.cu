@@ -176,13 +176,24 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
   bool done = false;
   while (iter <= a.itermax) {
     if (rho == 0.0) { warn |= VEBI_WARN_BICGSTAB_BREAKDOWN; done = true; break; }
-    // p = r + beta (p - omega v)
+    // p = r + beta (p - omega v).  The vector passes take rows i and i + stride per thread (the
+    // rows a thread owns do not change) and issue their loads before their stores: the compiler
+    // cannot move a load of one array above a store to another that may alias it.
     const double beta = rho / (rho0 + 1.0e-15) * alpha / (omega + 1.0e-15);
     acc = 0.0;
-    for (int i = tid; i < n; i += stride) {
-      double pi = (iter == 1) ? a.r[i] : fma(beta, fma(-omega, a.v[i], a.p[i]), a.r[i]);
+    for (int i = tid; i < n; i += 2 * stride) {
+      const int j = i + stride;
+      const bool h = j < n;
+      const double ri = a.r[i], vi = a.v[i], pi0 = a.p[i];
+      const double rj = h ? a.r[j] : 0.0, vj = h ? a.v[j] : 0.0, pj0 = h ? a.p[j] : 0.0;
+      const double pi = (iter == 1) ? ri : fma(beta, fma(-omega, vi, pi0), ri);
       a.p[i] = pi;
       acc += pi;
+      if (h) {
+        const double pj = (iter == 1) ? rj : fma(beta, fma(-omega, vj, pj0), rj);
+        a.p[j] = pj;
+        acc += pj;
+      }
     }
     double* slot = part;
     if (NONULL) {
@@ -214,11 +225,21 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
     // s = r - alpha v ; |s|^2 ; sum(s)
     double a2 = 0.0;
     acc = 0.0;
-    for (int i = tid; i < n; i += stride) {
-      double si = fma(-alpha, a.v[i], a.r[i]);
+    for (int i = tid; i < n; i += 2 * stride) {
+      const int j = i + stride;
+      const bool h = j < n;
+      const double vi = a.v[i], ri = a.r[i];
+      const double vj = h ? a.v[j] : 0.0, rj = h ? a.r[j] : 0.0;
+      const double si = fma(-alpha, vi, ri);
       a.s[i] = si;
       acc = fma(si, si, acc);
       a2 += si;
+      if (h) {
+        const double sj = fma(-alpha, vj, rj);
+        a.s[j] = sj;
+        acc = fma(sj, sj, acc);
+        a2 += sj;
+      }
     }
     slot = part + 4 * (size_t)nb;
     write_partials(acc, a2, 2, slot, sh);
@@ -257,12 +278,24 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
     // x, r update ; |r|^2 ; (r_bar, r) for the next rho
     acc = 0.0;
     a2 = 0.0;
-    for (int i = tid; i < n; i += stride) {
-      a.x[i] = fma(omega, a.sinv[i], fma(alpha, a.pinv[i], a.x[i]));
-      double ri = fma(-omega, a.t[i], a.s[i]);
+    for (int i = tid; i < n; i += 2 * stride) {
+      const int j = i + stride;
+      const bool h = j < n;
+      const double sii = a.sinv[i], pii = a.pinv[i], xi = a.x[i], ti = a.t[i], s_i = a.s[i], rbi = a.rb[i];
+      const double sij = h ? a.sinv[j] : 0.0, pij = h ? a.pinv[j] : 0.0, xj = h ? a.x[j] : 0.0;
+      const double tj = h ? a.t[j] : 0.0, s_j = h ? a.s[j] : 0.0, rbj = h ? a.rb[j] : 0.0;
+      a.x[i] = fma(omega, sii, fma(alpha, pii, xi));
+      const double ri = fma(-omega, ti, s_i);
       a.r[i] = ri;
       acc = fma(ri, ri, acc);
-      a2 = fma(a.rb[i], ri, a2);
+      a2 = fma(rbi, ri, a2);
+      if (h) {
+        a.x[j] = fma(omega, sij, fma(alpha, pij, xj));
+        const double rj = fma(-omega, tj, s_j);
+        a.r[j] = rj;
+        acc = fma(rj, rj, acc);
+        a2 = fma(rbj, rj, a2);
+      }
     }
     slot = part + 8 * (size_t)nb;
     write_partials(acc, a2, 2, slot, sh);
