@@ -1,0 +1,23 @@
+"""The barrier-profile analysis (vebisph_gb300/barrier_profile.py) on synthetic timestamps:
+per barrier position of a period, the mean work before it and the wait in it."""
+import numpy as np
+
+from vebisph_gb300.barrier_profile import phases
+
+
+def test_phases_recover_work_and_wait():
+    period, iters = 3, 4
+    work = np.array([10.0, 20.0, 30.0]) * 1e3  # ns
+    wait = np.array([1.0, 2.0, 3.0]) * 1e3
+    arrive, leave = [0.0], [500.0]  # the solve's first barrier
+    t = 500.0
+    for _ in range(iters):
+        for q in range(period):
+            t += work[q]
+            arrive.append(t)
+            t += wait[q]
+            leave.append(t)
+    out = phases(np.array(arrive), np.array(leave), period)
+    assert out["iterations"] == iters
+    assert np.allclose(out["work_us"], [10.0, 20.0, 30.0])
+    assert np.allclose(out["wait_us"], [1.0, 2.0, 3.0])

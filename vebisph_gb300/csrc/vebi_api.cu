@@ -1,5 +1,6 @@
 // vebi_api.cu -- the C-ABI of include/vebi.h: context set-up, state transfer, the step
 // orchestration (div_free, div_free.F90:22-124) and the inspection entry points.
+#include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -560,6 +561,18 @@ int vebi_run_steps(vebi_ctx* h, double x_mint, double y_mint, double x_maxt, dou
   return st;
 }
 
+// Wait for a stream by polling, for up to a second, before falling back to a blocking
+// synchronize: the copies of a download take ~2 ms, and a blocking wait can return tens of ms
+// late (measured on the Grace host) when the waiting thread is not woken promptly.
+static cudaError_t wait_stream_polling(cudaStream_t st) {
+  const auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    const cudaError_t e = cudaStreamQuery(st);
+    if (e != cudaErrorNotReady) return e;
+    if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(1)) return cudaStreamSynchronize(st);
+  }
+}
+
 int vebi_download_state(vebi_ctx* h, double* r, double* u, double* tau_p, double* theta, double* p, double* vort,
                         double* a_out, double* trace_conf, int32_t* n_surf, uint8_t* inbin, int32_t ld) {
   if (!h) return fail(VEBI_ERR_ARG, "null context");
@@ -585,7 +598,7 @@ int vebi_download_state(vebi_ctx* h, double* r, double* u, double* tau_p, double
   if (trace_conf) CUDA_TRY(cudaMemcpyAsync(trace_conf, d.trace_conf, B, cudaMemcpyDeviceToHost, x.st));
   if (n_surf) CUDA_TRY(cudaMemcpyAsync(n_surf, d.n_surf, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, x.st));
   if (inbin) CUDA_TRY(cudaMemcpyAsync(inbin, d.inbin, (size_t)n, cudaMemcpyDeviceToHost, x.st));
-  CUDA_TRY(cudaStreamSynchronize(x.st));
+  CUDA_TRY(wait_stream_polling(x.st));
   return VEBI_OK;
 }
 
