@@ -313,12 +313,13 @@ def run_gb300(args, dist: Dist):
     if mg:
         kname = ("k_bicgstab_mixed_mg<true>" if prec == abi.PREC_MIXED else "k_bicgstab_mg<true>") + \
             " (persistent cooperative BiCGSTAB with the multigrid V-cycle; the set-up kernels are in the stage time)"
-    if prec == abi.PREC_MIXED:
-        traffic = None
-    elif mg:
-        tmg = ROOT / "profiles" / "traffic_bicgstab_multigrid.json"
+    if mg:  # measured DRAM bytes per row-iteration of the preconditioned solvers at 1M rows
+        tmg = ROOT / "profiles" / ("traffic_bicgstab_multigrid_mixed.json" if prec == abi.PREC_MIXED
+                                   else "traffic_bicgstab_multigrid.json")
         traffic = (json.loads(tmg.read_text())["dram_bytes_per_row_iteration"] * case.npfb * iters_per_step
                    if tmg.exists() else None)
+    elif prec == abi.PREC_MIXED:
+        traffic = None
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
             "kernel": kname,

@@ -198,7 +198,6 @@ __global__ void __launch_bounds__(TPB) k_neighbours(Consts c, Dev d) {
   const bool mine = i < c.npfb;  // every lane stays to the warp reduction at the end
   int cnt = 0;
   if (mine && !d.inbin[i] && d.cellpart[i] >= 0) {
-    const double xi = d.rx[i], yi = d.ry[i];
     const float4 po = d.pk[i];
     const float S = (float)c.cell_size;
     const float S2 = (float)c.sup_size_2;
@@ -239,10 +238,11 @@ __global__ void __launch_bounds__(TPB) k_neighbours(Consts c, Dev d) {
           const float qq = fmaf(f1, f1, f2 * f2);
           const int j = __float_as_int(pv[u].z);
           // decided in FP32 far from both thresholds; the branch below is taken only inside
-          // the bands (and for the particle itself), so the common path does not diverge
+          // the bands, so the common path does not diverge.  The particle itself (r^2 = 0,
+          // never taken) is recognised by its index.
           bool take = (qq < lo) & (qq > band);
-          if ((qq <= hi) & !take) {  // near a threshold: the reference's FP64 test
-            const double r1 = xi - d.rx[j], r2 = yi - d.ry[j];
+          if ((qq <= hi) & !take & (j != i)) {  // near a threshold: the reference's FP64 test
+            const double r1 = d.rx[i] - d.rx[j], r2 = d.ry[i] - d.ry[j];
             const double rr2 = r1 * r1 + r2 * r2;
             take = rr2 > 0.0 && rr2 <= c.sup_size_2;
           }
