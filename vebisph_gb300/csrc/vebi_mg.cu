@@ -180,55 +180,71 @@ __global__ void k_mg_coarsen(MgLevel F, MgLevel G, Scal* s) {
 }
 
 // The coarsest level's dense inverse, for a direct coarse solve in the V-cycle: Gauss-Jordan
-// with partial pivoting in one warp, row r in lane r (at most MG_COARSEST = 32 rows).  A
-// closed domain's coarse matrix is singular (its rows sum to zero: the constant is in its null
-// space), so it is inverted as M + alpha 1 1^T with alpha = mean |diag| / n, which moves that
-// eigenvalue to mean |diag| and leaves the mean-free solution of M x = b unchanged.  *ok = 0
-// (a zero pivot, or a level too large) makes the V-cycle fall back to Jacobi sweeps.
-__global__ void __launch_bounds__(32) k_mg_coarse_inverse(MgLevel K, double* inv, int* ok, int closed) {
+// with partial pivoting in one 32 x 32 block, thread (ty, tx) owning row ty and columns tx and
+// tx + 32 of [M | I] (at most MG_COARSEST = 32 rows).  A closed domain's coarse matrix is
+// singular (its rows sum to zero: the constant is in its null space), so it is inverted as
+// M + alpha 1 1^T with alpha = mean |diag| / n, which moves that eigenvalue to mean |diag| and
+// leaves the mean-free solution of M x = b unchanged.  *ok = 0 (a zero pivot, or a level too
+// large) makes the V-cycle fall back to Jacobi sweeps.
+__global__ void __launch_bounds__(1024) k_mg_coarse_inverse(MgLevel K, double* inv, int* ok, int closed) {
   __shared__ double M[MG_COARSEST][2 * MG_COARSEST + 1];
-  const int n = K.n, r = threadIdx.x;
+  __shared__ double fcol[MG_COARSEST];
+  __shared__ int piv_row;
+  __shared__ double alpha_s;
+  const int n = K.n, tx = threadIdx.x, ty = threadIdx.y;
   if (n > MG_COARSEST || n < 1) {
-    if (r == 0) *ok = 0;
+    if (tx == 0 && ty == 0) *ok = 0;
     return;
   }
-  double ad = r < n ? fabs(K.diag[r]) : 0.0;
-  for (int o = 16; o > 0; o >>= 1) ad += __shfl_xor_sync(0xffffffffu, ad, o);
-  const double alpha = closed ? ad / ((double)n * (double)n) : 0.0;
-  if (r < n) {
-    for (int c = 0; c < 2 * n; ++c) M[r][c] = (c < n ? alpha : 0.0);
+  if (ty == 0) {  // alpha from the warp of row-owners
+    double ad = tx < n ? fabs(K.diag[tx]) : 0.0;
+    for (int o = 16; o > 0; o >>= 1) ad += __shfl_xor_sync(0xffffffffu, ad, o);
+    if (tx == 0) alpha_s = closed ? ad / ((double)n * (double)n) : 0.0;
+  }
+  __syncthreads();
+  const int r = ty;
+  if (r < n)
+    for (int c = tx; c < 2 * n; c += 32) M[r][c] = c < n ? alpha_s : (c - n == r ? 1.0 : 0.0);
+  __syncthreads();
+  if (r < n && tx == 0) {
     M[r][r] += K.diag[r];
-    M[r][n + r] = 1.0;
     const int m = K.cnt[r];
     for (int t = 0; t < m; ++t) M[r][K.col[(size_t)t * K.n + r]] += K.val[(size_t)t * K.n + r];
   }
-  __syncwarp();
+  __syncthreads();
   bool good = true;
   for (int k = 0; k < n; ++k) {
-    double v = (r >= k && r < n) ? fabs(M[r][k]) : -1.0;
-    int p = r;
-    for (int o = 16; o > 0; o >>= 1) {  // argmax, ties to the lower row
-      const double v2 = __shfl_xor_sync(0xffffffffu, v, o);
-      const int p2 = __shfl_xor_sync(0xffffffffu, p, o);
-      if (v2 > v || (v2 == v && p2 < p)) { v = v2; p = p2; }
+    if (ty == 0) {  // argmax of |M[i][k]| over i >= k, ties to the lower row
+      double v = (tx >= k && tx < n) ? fabs(M[tx][k]) : -1.0;
+      int p = tx;
+      for (int o = 16; o > 0; o >>= 1) {
+        const double v2 = __shfl_xor_sync(0xffffffffu, v, o);
+        const int p2 = __shfl_xor_sync(0xffffffffu, p, o);
+        if (v2 > v || (v2 == v && p2 < p)) { v = v2; p = p2; }
+      }
+      if (tx == 0) piv_row = v > 0.0 ? p : -1;
     }
-    if (!(v > 0.0)) { good = false; break; }
-    if (p != k)
-      for (int c = r; c < 2 * n; c += 32) { const double t = M[k][c]; M[k][c] = M[p][c]; M[p][c] = t; }
-    __syncwarp();
+    __syncthreads();
+    const int p = piv_row;
+    if (p < 0) { good = false; break; }
+    if (ty == 0 && p != k)
+      for (int c = tx; c < 2 * n; c += 32) { const double t = M[k][c]; M[k][c] = M[p][c]; M[p][c] = t; }
+    __syncthreads();
     const double piv = M[k][k];
-    __syncwarp();
-    for (int c = r; c < 2 * n; c += 32) M[k][c] /= piv;
-    __syncwarp();
+    __syncthreads();
+    if (ty == 0)
+      for (int c = tx; c < 2 * n; c += 32) M[k][c] /= piv;
+    if (tx == 0 && r < n) fcol[r] = M[r][k];
+    __syncthreads();
     if (r < n && r != k) {
-      const double f = M[r][k];
-      for (int c = 0; c < 2 * n; ++c) M[r][c] = fma(-f, M[k][c], M[r][c]);
+      const double f = fcol[r];
+      for (int c = tx; c < 2 * n; c += 32) M[r][c] = fma(-f, M[k][c], M[r][c]);
     }
-    __syncwarp();
+    __syncthreads();
   }
   if (good && r < n)
-    for (int c = 0; c < n; ++c) inv[(size_t)r * n + c] = M[r][n + c];
-  if (r == 0) *ok = good ? 1 : 0;
+    for (int c = tx; c < n; c += 32) inv[(size_t)r * n + c] = M[r][n + c];
+  if (tx == 0 && ty == 0) *ok = good ? 1 : 0;
 }
 
 // sum over a row's cell pairs t = t_first..m-1 of (A P)_ic (g_c - g_own), in pair order,
@@ -1111,7 +1127,8 @@ static int mg_setup(Ctx& x) {
   VEBI_LAUNCH(x, k_mg_level1, grid_for(x.mg[0].n), TPB, c, x.d, x.mg[0], x.mg_ragg, x.mg_rval, x.mg_rcnt);
   for (int l = 0; l + 1 < nl; ++l)
     VEBI_LAUNCH(x, k_mg_coarsen, grid_for(x.mg[l + 1].n), TPB, x.mg[l], x.mg[l + 1], x.d.s);
-  VEBI_LAUNCH(x, k_mg_coarse_inverse, 1, 32, x.mg[nl - 1], x.mg_kinv, x.mg_kinv_ok, c.open_domain == 0 ? 1 : 0);
+  VEBI_LAUNCH(x, k_mg_coarse_inverse, 1, dim3(32, 32), x.mg[nl - 1], x.mg_kinv, x.mg_kinv_ok,
+              c.open_domain == 0 ? 1 : 0);
   int tail = nl - 1;
   for (int l = 0; l < nl; ++l)
     if (x.mg[l].n <= x.mg_block_rows) { tail = l; break; }
