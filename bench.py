@@ -344,6 +344,7 @@ def run_gb300(args, dist: Dist):
         h2d = sum(host[k].nbytes for k in ("r", "u", "tau", "theta", "trace_conf", "inbin"))
         d2h = sum(host[k].nbytes for k in ("r", "u", "tau", "theta", "trace_conf", "inbin", "p"))
         t_up = t_step = t_down = 0.0
+        down_ms = []
         dist.barrier()
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
@@ -357,6 +358,7 @@ def run_gb300(args, dist: Dist):
                                         host["inbin"].ctypes.data_as(C.POINTER(C.c_uint8)), n)
             td = time.perf_counter()
             t_up, t_step, t_down = t_up + tb - ta, t_step + tc - tb, t_down + td - tc
+            down_ms.append(round(1e3 * (td - tc), 2))
         e2e_s = time.perf_counter() - t0
         dist.barrier()
         e2e_s = dist.max(e2e_s)
@@ -369,6 +371,7 @@ def run_gb300(args, dist: Dist):
                "host_pinned": pinned_ok,
                "ms_per_step": {"upload_call": round(1e3 * t_up / k, 3), "step": round(1e3 * t_step / k, 3),
                                "download": round(1e3 * t_down / k, 3)},
+               "download_ms_each_step": down_ms,
                "path": "vebi_upload_state + vebi_step + vebi_download_state on pinned host arrays that carry "
                        "the state from step to step (upload is asynchronous; its copies complete inside the step "
                        "call, whose stats read-back waits for the stream)"}
