@@ -208,27 +208,31 @@ def stage_bandwidth(stage_ms_per_step: dict, n: int, kbar: float, mixed: bool, p
 def mg_bytes_per_iteration(n_rows: int, nnz_off: int, n_cells: int, mixed: bool = False,
                            pairs: float = 5.0) -> float:
     """Algorithmic bytes of one multigrid-preconditioned BiCGSTAB iteration (closed domain),
-    pass by pass; k = off-diagonal slots per row, p = (cell, value) pairs of A P per row.
+    pass by pass; k = off-diagonal slots per row.  `pairs` (the mean (cell, value) pairs of A P
+    per row) is reported beside the figure; the output pass reads A P by 3x3 direction, eight
+    values per row whatever the pair count.
 
-    BiCGSTAB passes, 184 B per row in both precisions: p update 32 (r, v, p; p), v 32 (w, row
-    sum, r_bar; v), s 24 (v, r; s), t 32 (w, row sum, s; t), x/r update 64 (the two
-    preconditioned directions, x, t, s, r_bar; x, r -- the directions are FP64 or FP32 (hi, lo)
-    pairs, 8 B either way).  The products A M^-1 p and A M^-1 s are the V-cycle's w.
+    BiCGSTAB passes: p update 32 (r, v, p; p), v (w, row sum, r_bar; v), s 24 (v, r; s), t (w,
+    row sum, s; t), x/r update 64 (the two preconditioned directions, x, t, s, r_bar; x, r).
+    The products A M^-1 p and A M^-1 s are the V-cycle's w: FP64 in the FP64 solver (v and t
+    32 B each, 184 B in all), FP32 in the mixed one (28 B each, 176 B in all).
     Two V-cycles, particle level:
-      mean removal and first sweep: FP64 32 B (q, 1/diag; q, z), mixed 24 (FP32 1/diag and z);
-      residual: FP64 36 + 12k (count, diagonal, z_i, q; fr), mixed 28 + 8k (count, row sum,
-        FP32 z_i, q; FP32 fr);
+      mean removal and first sweep: FP64 32 B (q, 1/diag; q, z), mixed 28 (q, FP32 1/diag; q,
+        FP32 q and z);
+      residual: FP64 36 + 12k (count, diagonal, z_i, q; fr), mixed 20 + 8k (count, FP32 row
+        sum, z_i and q; FP32 fr);
       restriction: FP64 12, mixed 8 (cell list entry, fr);
-      output: FP64 56, mixed 48 (cell, pair count, z, fr, q, row sum; the direction and w) plus
-        12 B per pair beyond the row's own cell.
+      output: FP64 120 (cell, packed word, z, fr, q, row sum, eight FP64 direction values; the
+        direction and w), mixed 68 (the same in FP32 but the FP64 direction, and w in FP32).
     Coarse levels: ~390 B per cell (the cell level's ELL rows read by the residual and the
     smoothing sweep, work vectors, and the geometric sum of the coarser levels)."""
-    extra_pairs = 12.0 * max(pairs - 1.0, 0.0) * n_rows
     if mixed:
-        fine = 8.0 * nnz_off + (24.0 + 28.0 + 8.0 + 48.0) * n_rows + extra_pairs
+        fine = 8.0 * nnz_off + (28.0 + 20.0 + 8.0 + 68.0) * n_rows
+        krylov = 176.0
     else:
-        fine = 12.0 * nnz_off + (32.0 + 36.0 + 12.0 + 56.0) * n_rows + extra_pairs
-    return 184.0 * n_rows + 2.0 * (fine + 390.0 * n_cells)
+        fine = 12.0 * nnz_off + (32.0 + 36.0 + 12.0 + 120.0) * n_rows
+        krylov = 184.0
+    return krylov * n_rows + 2.0 * (fine + 390.0 * n_cells)
 
 
 def cpu_baseline(case, gpu_iters_per_step: float, itermax_sample: int):

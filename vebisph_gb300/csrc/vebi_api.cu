@@ -276,6 +276,7 @@ static int allocate_all(Ctx& x) {
     cudaMemcpy(x.d_mg, x.mg.data(), sizeof(MgLevel) * x.mg.size(), cudaMemcpyHostToDevice);
     A_(x.mg_z, n); A_(x.mg_fr, n); A_(x.mg_dinv0, n); A_(x.mg_rsum, n); A_(x.mg_w, n);
     A_(x.mg_ragg, n * MG_ROW_SLOTS); A_(x.mg_rval, n * MG_ROW_SLOTS); A_(x.mg_rcnt, n);
+    A_(x.mg_rv9, n * 8); A_(x.mg_rx, n); A_(x.mg_g32, (size_t)x.mg[0].n); A_(x.mg_q32, n);
     A_(x.mg_kinv, (size_t)MG_COARSEST * MG_COARSEST); A_(x.mg_kinv_ok, 1);
   }
 #undef A_

@@ -47,6 +47,12 @@ struct Ctx {
   double* mg_kinv = nullptr;       // dense inverse of the coarsest level
   int* mg_kinv_ok = nullptr;
   double* mg_rval = nullptr;
+  // the same rows by 3x3 direction for the V-cycle's output pass: values [8][n] (own cell
+  // excluded, zero where unused) and a packed word per row (list start | count << 8 | used << 16)
+  double* mg_rv9 = nullptr;
+  int* mg_rx = nullptr;
+  float* mg_g32 = nullptr;         // mixed precision: the level-1 solution rounded to FP32
+  float* mg_q32 = nullptr;         // mixed precision: the V-cycle's input rounded to FP32
   std::vector<void*> allocs;
   DumpState* dump = nullptr;       // output staging (vebi_output.cu), made at the first dump
   // adjoint window (vebi_adjoint.cu): right after advection a step records its geometry --

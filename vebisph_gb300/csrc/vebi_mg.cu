@@ -68,15 +68,29 @@ __device__ __forceinline__ void slot_store(const MgLevel& L, int row, const int*
 // any other cell goes to a short searched list.  Each cell's sum runs in slot order, as a
 // searched table's would; the pairs come out own cell first, then the 3x3 in key order, then
 // the list.
+//
+// The same sums also go out by direction for the output pass of the V-cycle: rv9[k][i] for the
+// eight directions q = 0..8 without the own cell (k = q, or q - 1 past it), zero where the row
+// has no column, and rx[i] = (first list slot) | (pair count << 8) | (used directions << 16).
+// The output pass then computes every gather address from the row's own cell, without a
+// dependent load of the pair's cell.  With val32 (mixed precision) the direction values are
+// FP32, rv9 read as float [8][npfb].
 __global__ void __launch_bounds__(TPB) k_mg_rows(Consts c, Dev d, const float* __restrict__ val32,
                                                  int* __restrict__ ragg, double* __restrict__ rval,
-                                                 int* __restrict__ rcnt) {
+                                                 int* __restrict__ rcnt, double* __restrict__ rv9,
+                                                 int* __restrict__ rx) {
   __shared__ double nb9[9][TPB];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.npfb) return;
   const int own = d.cellpart[i];
   if (own < 0) {  // a binned particle belongs to no cell
     rcnt[i] = 0;
+    rx[i] = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (val32) ((float*)rv9)[(size_t)k * c.npfb + i] = 0.f;
+      else rv9[(size_t)k * c.npfb + i] = 0.0;
+    }
     return;
   }
   double* acc = &nb9[0][threadIdx.x];  // slot q at acc[q * TPB]
@@ -111,18 +125,27 @@ __global__ void __launch_bounds__(TPB) k_mg_rows(Consts c, Dev d, const float* _
   ragg[i] = own;
   rval[i] = acc[4 * TPB];
   ++t;
+  unsigned used8 = 0;
 #pragma unroll
   for (int q = 0; q < 9; ++q) {
-    if (q == 4 || !(used & (1u << q))) continue;
+    if (q == 4) continue;
+    const int k = q < 4 ? q : q - 1;
+    const bool u = (used & (1u << q)) != 0;
+    if (val32) ((float*)rv9)[(size_t)k * c.npfb + i] = u ? (float)acc[q * TPB] : 0.f;
+    else rv9[(size_t)k * c.npfb + i] = u ? acc[q * TPB] : 0.0;
+    if (!u) continue;
+    used8 |= 1u << k;
     ragg[(size_t)t * c.npfb + i] = own + (q / 3 - 1) * ncx + (q % 3 - 1);
     rval[(size_t)t * c.npfb + i] = acc[q * TPB];
     ++t;
   }
+  const int t_list = t;
   for (int e = 0; e < m; ++e, ++t) {
     ragg[(size_t)t * c.npfb + i] = tc[e];
     rval[(size_t)t * c.npfb + i] = tv[e];
   }
   rcnt[i] = t;
+  rx[i] = t_list | (t << 8) | (int)(used8 << 16);
   if (!ok) d.s->mg_fail = 1;
 }
 
@@ -272,40 +295,28 @@ __device__ __forceinline__ double ap_pairs(const int* __restrict__ ragg, const d
   return ap;
 }
 
-// The first four pairs beyond the row's own cell, loaded without waiting for the row's pair
-// count: the pair table has MG_ROW_SLOTS slots for every row, so slots past the count are in
-// bounds; they are masked once the count is known.  Most rows have at most five pairs, so the
-// row's loads form one round trip and the gathers of g a second.
-struct ApHead {
-  int c[4];
-  double v[4];
-};
-
-__device__ __forceinline__ ApHead ap_head(const int* __restrict__ ragg, const double* __restrict__ rval, size_t i,
-                                          size_t n) {
-  ApHead h;
+// rowsum_i g_own + sum_c (A P)_ic (g_c - g_own) for row i from its direction table: the eight
+// neighbour cells' values and gathers are all issued at once, their addresses computed from the
+// row's own cell (`own`, with g[own] = gc); unused directions gather g[own] and add nothing.  The
+// sum runs in the pair order of k_mg_rows (the 3x3 in key order, then the row's searched list).
+__device__ __forceinline__ double ap_stencil(const double* __restrict__ rv9, const int* __restrict__ ragg,
+                                             const double* __restrict__ rval, int rx, size_t i, size_t n,
+                                             const double* g, int own, int ncx, double gc, double rs) {
+  const unsigned used = ((unsigned)rx >> 16) & 0xffu;
+  double v8[8], g8[8];
 #pragma unroll
-  for (int u = 0; u < 4; ++u) {
-    h.c[u] = __ldg(ragg + (size_t)(1 + u) * n + i);
-    h.v[u] = __ldg(rval + (size_t)(1 + u) * n + i);
+  for (int k = 0; k < 8; ++k) {
+    const int q = k < 4 ? k : k + 1;
+    const int off = (q / 3 - 1) * ncx + (q % 3 - 1);
+    v8[k] = __ldg(rv9 + (size_t)k * n + i);
+    g8[k] = g[(used >> k) & 1u ? own + off : own];
   }
-  return h;
-}
-
-// rowsum_i g_own + sum_c (A P)_ic (g_c - g_own) from a prefetched head and the row's count m;
-// own = the row's cell, whose value g[own] = gc.  Masked slots gather g[own]: an index read
-// past the row's count is never used as an address.
-__device__ __forceinline__ double ap_row(const ApHead& h, const int* __restrict__ ragg,
-                                         const double* __restrict__ rval, int m, size_t i, size_t n,
-                                         const double* g, int own, double gc, double rs) {
-  double g4[4];
-#pragma unroll
-  for (int u = 0; u < 4; ++u) g4[u] = g[1 + u < m ? h.c[u] : own];
   double ap = rs * gc;
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
-    if (1 + u < m) ap = fma(h.v[u], g4[u] - gc, ap);
-  if (m > 5) ap = ap_pairs(ragg, rval, m, i, n, g, gc, ap, 5);
+  for (int k = 0; k < 8; ++k)
+    if ((used >> k) & 1u) ap = fma(v8[k], g8[k] - gc, ap);
+  const int t0 = rx & 0xff, m = (rx >> 8) & 0xff;
+  if (t0 < m) ap = ap_pairs(ragg, rval, m, i, n, g, gc, ap, t0);
   return ap;
 }
 
@@ -317,13 +328,15 @@ struct MgArgs {
   int tail;                  // first level handled by block 0 alone
   const int *agg, *cstart, *ccnt, *ip;  // fine aggregate (cell) of each row; cell lists
   double *z, *fr, *dinv0, *rsum;        // fine work vectors, 1/diag, row sums
-  // A P by fine row: (cell, sum of the row's values in that cell) pairs, own cell first
-  // (k_mg_rows), and A times the V-cycle's output
-  const int *ragg, *rcnt;
-  const double* rval;
+  // A P by fine row (k_mg_rows): (cell, sum of the row's values in that cell) pairs, own cell
+  // first, and the same by 3x3 direction with the packed word; A times the V-cycle's output
+  const int *ragg, *rx;
+  const double *rval, *rv9;
+  int ncx;
   double* w;
   const double* kinv;        // the coarsest level's dense inverse, if *kinv_ok
   const int* kinv_ok;
+  float* g32;                // mixed precision: the level-1 solution rounded to FP32, else null
 };
 
 // (A x)_c on a coarse level; x may have been written by other blocks in this launch
@@ -359,10 +372,74 @@ __device__ __forceinline__ void lv_prolong(const MgLevel& F, const double* gsol,
   }
 }
 
-// one damped Jacobi sweep of x into r
-__device__ __forceinline__ void lv_smooth(const MgLevel& L, int i0, int st) {
-  for (int c = i0; c < L.n; c += st)
-    L.r[c] = fma(MG_OMEGA * __ldg(L.dinv + c), L.b[c] - lv_Ax(L, L.x, c), L.x[c]);
+// one damped Jacobi sweep of x into r, and into x32 rounded to FP32 when given
+__device__ __forceinline__ void lv_smooth(const MgLevel& L, int i0, int st, float* x32 = nullptr) {
+  for (int c = i0; c < L.n; c += st) {
+    const double v = fma(MG_OMEGA * __ldg(L.dinv + c), L.b[c] - lv_Ax(L, L.x, c), L.x[c]);
+    L.r[c] = v;
+    if (x32) x32[c] = (float)v;
+  }
+}
+
+// The grid-wide levels fuse each pair of phases, so a level costs one grid barrier on the way
+// down and one on the way up; both give the same bits as the two phases in sequence.
+//
+// Down: F's residual and its restriction into G.  Four consecutive lanes take the four children
+// of one coarse row; their residuals are summed by shuffles in child order, as lv_restrict sums
+// F.r.  The loop bound is warp-uniform (the shuffles need every lane).
+__device__ __forceinline__ void lv_residual_restrict(const MgLevel& F, const MgLevel& G, int i0, int st) {
+  const int lane = threadIdx.x & 31;
+  const int total = 4 * G.n;
+  for (int t0 = i0 - lane; t0 < total; t0 += st) {
+    const int t = t0 + lane;
+    const int C = t >> 2, q = t & 3;
+    double r = 0.0;
+    int ok = 0;
+    if (t < total) {
+      const int X = C % G.gx, Y = C / G.gx;
+      const int fx = 2 * X + (q & 1), fy = 2 * Y + (q >> 1);
+      if (fx < F.gx && fy < F.gy) {
+        const int f = fx + fy * F.gx;
+        r = F.b[f] - lv_Ax(F, F.x, f);
+        ok = 1;
+      }
+    }
+    const double r1 = __shfl_down_sync(0xffffffffu, r, 1);
+    const double r2 = __shfl_down_sync(0xffffffffu, r, 2);
+    const double r3 = __shfl_down_sync(0xffffffffu, r, 3);
+    const int okm = ok | (__shfl_down_sync(0xffffffffu, ok, 1) << 1) | (__shfl_down_sync(0xffffffffu, ok, 2) << 2) |
+                    (__shfl_down_sync(0xffffffffu, ok, 3) << 3);
+    if (q == 0 && t < total) {
+      double b = 0.0;
+      if (okm & 1) b += r;
+      if (okm & 2) b += r1;
+      if (okm & 4) b += r2;
+      if (okm & 8) b += r3;
+      G.b[C] = b;
+      G.x[C] = MG_OMEGA * __ldg(G.dinv + C) * b;
+    }
+  }
+}
+
+// Up: prolongation of G's solution into F and F's smoothing sweep.  Each row forms the
+// prolonged x of itself and of its columns from F.x and gsol (neither written in this phase) and
+// writes the smoothed value into r (and x32 rounded to FP32 when given); F.x itself is left
+// as it was, which nothing reads afterwards.
+__device__ __forceinline__ void lv_prolong_smooth(const MgLevel& F, const double* gsol, int ggx, int i0, int st,
+                                                  float* x32 = nullptr) {
+  for (int c = i0; c < F.n; c += st) {
+    auto xp = [&](int k) {
+      const int X = (k % F.gx) >> 1, Y = (k / F.gx) >> 1;
+      return fma(MG_GAMMA, gsol[X + Y * ggx], F.x[k]);
+    };
+    const double xc = xp(c);
+    double y = __ldg(F.diag + c) * xc;
+    const int m = __ldg(F.cnt + c);
+    for (int t = 0; t < m; ++t) y = fma(__ldg(F.val + (size_t)t * F.n + c), xp(__ldg(F.col + (size_t)t * F.n + c)), y);
+    const double v = fma(MG_OMEGA * __ldg(F.dinv + c), F.b[c] - y, xc);
+    F.r[c] = v;
+    if (x32) x32[c] = (float)v;
+  }
 }
 
 // the solution of level l after the upward pass: post-smoothed into r, or x on the coarsest
@@ -396,11 +473,15 @@ __device__ void mg_block_levels(const MgArgs& a) {
       __syncthreads();
     }
   }
+  if (a.g32 && a.nl == 1) {  // level 1 is the coarsest
+    for (int c = i0; c < K.n; c += st) a.g32[c] = (float)K.x[c];
+    __syncthreads();
+  }
   for (int l = a.nl - 2; l >= a.tail; --l) {
     const MgLevel F = a.lv[l];
     lv_prolong(F, lv_sol(a, l + 1), a.lv[l + 1].gx, i0, st);
     __syncthreads();
-    lv_smooth(F, i0, st);
+    lv_smooth(F, i0, st, l == 0 ? a.g32 : nullptr);
     __syncthreads();
   }
 }
@@ -445,36 +526,47 @@ __device__ bool mg_vcycle(const MgArgs& a, double* q, double qshift, double* out
   }
   if (!grid_sync(s)) return false;
   for (int l = 0; l < a.tail; ++l) {
-    const MgLevel F = a.lv[l], G = a.lv[l + 1];
-    lv_residual(F, tid, stride);
-    if (!grid_sync(s)) return false;
-    lv_restrict(F, G, tid, stride);
+    lv_residual_restrict(a.lv[l], a.lv[l + 1], tid, stride);
     if (!grid_sync(s)) return false;
   }
   if (blockIdx.x == 0) mg_block_levels(a);
   if (!grid_sync(s)) return false;
   for (int l = a.tail - 1; l >= 0; --l) {
-    const MgLevel F = a.lv[l];
-    lv_prolong(F, lv_sol(a, l + 1), a.lv[l + 1].gx, tid, stride);
-    if (!grid_sync(s)) return false;
-    lv_smooth(F, tid, stride);
+    lv_prolong_smooth(a.lv[l], lv_sol(a, l + 1), a.lv[l + 1].gx, tid, stride);
     if (!grid_sync(s)) return false;
   }
   // prolongation to the particles (the particle level is pre-smoothed only), and
   // w = A out = A z + gamma (A P) g1 with A z = q - fr from the fine residual and (A P) g1 in
   // difference form over the row's cell pairs: rowsum_i g_own + sum_c (AP)_ic (g_c - g_own)
+  // Software-pipelined: a row's streamed operands are loaded one pass ahead, together with the
+  // gathers of the row before, so each pass waits for one round trip to memory, not two.
   const double* g1 = lv_sol(a, 0);
   double acc = 0.0;
+  struct Row {
+    int c, rx;
+    double z, q, fr, rs;
+  };
+  auto load_row = [&](int i) {
+    Row r;
+    r.c = __ldg(a.agg + i);
+    r.rx = __ldg(a.rx + i);
+    r.z = z[i];
+    r.q = q[i];
+    r.fr = a.fr[i];
+    r.rs = a.rsum[i];
+    return r;
+  };
+  Row cur{};
+  if (tid < n) cur = load_row(tid);
   for (int i = tid; i < n; i += stride) {
-    const int c = __ldg(a.agg + i), mc = __ldg(a.rcnt + i);
-    const double zi = z[i], qi = q[i], fri = a.fr[i], rsi = a.rsum[i];
-    const ApHead hd = ap_head(a.ragg, a.rval, i, n);
-    double o = zi;
-    double w = qi - fri;
-    if (c >= 0) {
-      const double gc = g1[c];
+    const Row r = cur;
+    if (i + stride < n) cur = load_row(i + stride);
+    double o = r.z;
+    double w = r.q - r.fr;
+    if (r.c >= 0) {
+      const double gc = g1[r.c];
       o = fma(MG_GAMMA, gc, o);
-      w = fma(MG_GAMMA, ap_row(hd, a.ragg, a.rval, mc, i, n, g1, c, gc, rsi), w);
+      w = fma(MG_GAMMA, ap_stencil(a.rv9, a.ragg, a.rval, r.rx, i, n, g1, r.c, a.ncx, gc, r.rs), w);
     }
     out[i] = o;
     a.w[i] = w;
@@ -500,7 +592,7 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
   double* part = a.part;
   const double rinv1 = 1.0 / (1.0 + 1.0e-15);
   const double small = NONULL ? 1.0e-6 : 4.0;  // open solver: the integer expression 10-6
-  double red[2];
+  double red[4];
   double acc = 0.0;
   // out = M^-1 (q - qshift) with q -= qshift stored back (q: own rows complete), and the
   // block partial of sum(out) into slot
@@ -547,13 +639,14 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
   write_partials(acc, 0.0, 1, part + 10 * (size_t)nb, sh);
   if (!grid_sync(s)) return;
   reduce_partials(part + 10 * (size_t)nb, nb, 1, red, shv);
-  double rho = red[0], rho0 = 1.0, alpha = 1.0, omega = 1.0;
+  double rho = red[0], alpha = 1.0, omega = 1.0;
+  double beta = 0.0;  // for iteration 2 on, derived with the previous iteration's last reduction
+  const double dn = (double)n;
   double n2r0 = 1.0, n2s0 = 1.0, resid = 0.0;
   int iter = 1, warn = 0;
   bool done = false;
   while (iter <= a.itermax) {
     if (rho == 0.0) { warn |= VEBI_WARN_BICGSTAB_BREAKDOWN; done = true; break; }
-    const double beta = rho / (rho0 + 1.0e-15) * alpha / (omega + 1.0e-15);
     acc = 0.0;
     for (int i = tid; i < n; i += 2 * stride) {
       const int j = i + stride;
@@ -573,14 +666,14 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
     if (NONULL) {
       write_partials(acc, 0.0, 1, part, sh);
       if (!grid_sync(s)) return;
-      reduce_partials(part, nb, 1, red, shv);
-      mean = red[0] / (double)n;
+      reduce_partials(part, nb, 1, red, shv, [=](double* v) { v[0] = v[0] / dn; });
+      mean = red[0];
     }
     // p_hat = M^-1 (p - mean), made mean-free (closed domains) through mp
     if (!precond(a.p, mean, a.pinv, part + 1 * (size_t)nb)) return;
     if (!grid_sync(s)) return;
-    reduce_partials(part + 1 * (size_t)nb, nb, 1, red, shv);
-    const double mp = NONULL ? red[0] / (double)n : 0.0;
+    reduce_partials(part + 1 * (size_t)nb, nb, 1, red, shv, [=](double* v) { v[0] = NONULL ? v[0] / dn : 0.0; });
+    const double mp = red[0];
     // v = A (p_hat - mp) ; (r_bar, v)
     acc = 0.0;
     if (use_mg) {
@@ -607,8 +700,8 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
     }
     write_partials(acc, 0.0, 1, part + 2 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
-    reduce_partials(part + 2 * (size_t)nb, nb, 1, red, shv);
-    alpha = rho / (red[0] + 1.0e-15);
+    reduce_partials(part + 2 * (size_t)nb, nb, 1, red, shv, [=](double* v) { v[0] = rho / (v[0] + 1.0e-15); });
+    alpha = red[0];
     double a2 = 0.0;
     acc = 0.0;
     for (int i = tid; i < n; i += 2 * stride) {
@@ -629,9 +722,9 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
     }
     write_partials(acc, a2, 2, part + 4 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
-    reduce_partials(part + 4 * (size_t)nb, nb, 2, red, shv);
+    reduce_partials(part + 4 * (size_t)nb, nb, 2, red, shv, [=](double* v) { v[1] = v[1] / dn; });
     const double n2s = red[0];
-    const double mean_s = red[1] / (double)n;
+    const double mean_s = red[1];
     if (iter == 1) n2s0 = (n2s <= small) ? 1.0 : n2s;
     if (n2s <= a.tol * a.tol * n2s0) {
       for (int i = tid; i < n; i += stride) a.x[i] = fma(alpha, a.pinv[i] - mp, a.x[i]);
@@ -641,8 +734,8 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
     }
     if (!precond(a.s, NONULL ? mean_s : 0.0, a.sinv, part + 3 * (size_t)nb)) return;
     if (!grid_sync(s)) return;
-    reduce_partials(part + 3 * (size_t)nb, nb, 1, red, shv);
-    const double ms = NONULL ? red[0] / (double)n : 0.0;
+    reduce_partials(part + 3 * (size_t)nb, nb, 1, red, shv, [=](double* v) { v[0] = NONULL ? v[0] / dn : 0.0; });
+    const double ms = red[0];
     // t = A (s_hat - ms) ; (t, s) ; |t|^2
     acc = 0.0;
     a2 = 0.0;
@@ -673,8 +766,8 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
     }
     write_partials(acc, a2, 2, part + 6 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
-    reduce_partials(part + 6 * (size_t)nb, nb, 2, red, shv);
-    omega = red[0] / (red[1] + 1.0e-15);
+    reduce_partials(part + 6 * (size_t)nb, nb, 2, red, shv, [](double* v) { v[0] = v[0] / (v[1] + 1.0e-15); });
+    omega = red[0];
     acc = 0.0;
     a2 = 0.0;
     for (int i = tid; i < n; i += 2 * stride) {
@@ -698,14 +791,19 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
     }
     write_partials(acc, a2, 2, part + 8 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
-    reduce_partials(part + 8 * (size_t)nb, nb, 2, red, shv);
+    // v[2] = the relative residual, v[3] = the next iteration's beta from the new rho v[1]
+    reduce_partials(part + 8 * (size_t)nb, nb, 2, red, shv, [=](double* v) {
+      const double r0 = iter == 1 ? ((v[0] <= small) ? 1.0 : v[0]) : n2r0;
+      v[2] = sqrt(v[0] / r0);
+      v[3] = v[1] / (rho + 1.0e-15) * alpha / (omega + 1.0e-15);
+    });
     const double n2r = red[0];
     if (iter == 1) n2r0 = (n2r <= small) ? 1.0 : n2r;
-    resid = sqrt(n2r / n2r0);
+    resid = red[2];
     if (n2r <= a.tol * a.tol * n2r0) { done = true; break; }
     iter = iter + 1;
-    rho0 = rho;
     rho = red[1];
+    beta = red[3];
   }
   if (!done) warn |= VEBI_WARN_MAXITER;
   for (int i = tid; i < n; i += stride) a.P[i] = a.x[i];
@@ -729,15 +827,20 @@ struct MgMxArgs {
   int nl, tail;
   const int *agg, *cstart, *ccnt, *ip;
   float *z, *fr, *dinv0;
-  const int *ragg, *rcnt;  // A P by fine row, as in MgArgs
+  const int *ragg, *rx;  // A P by fine row, as in MgArgs, with FP32 direction values
   const double* rval;
-  double* w;               // A times the V-cycle's output
+  const float* rv9;
+  int ncx;
+  float* w;                // A times the V-cycle's output, FP32
   const double* kinv;      // the coarsest level's dense inverse, if *kinv_ok
   const int* kinv_ok;
+  float* g32;              // the level-1 solution rounded to FP32
+  float* rs32;             // the row sums rounded to FP32
+  float* q32;              // the V-cycle's input (after mean removal) rounded to FP32
 };
 
-// sum_k A_ik (z_col - z_i) + rowsum_i z_i in FP32 (one FP32 vector)
-__device__ __forceinline__ float spmv_diff32s(const MxArgs& a, const float* z, int i) {
+// sum_k A_ik (z_col - z_i) + rowsum_i z_i in FP32 (one FP32 vector; rs32 = FP32 row sums)
+__device__ __forceinline__ float spmv_diff32s(const MxArgs& a, const float* rs32, const float* z, int i) {
   const int cnt = __ldg(a.cnt + i);
   const float* vp = a.val32 + i;
   const int* cp = a.col + i;
@@ -760,44 +863,76 @@ __device__ __forceinline__ float spmv_diff32s(const MxArgs& a, const float* z, i
     cp += st;
     vp += st;
   }
-  return fmaf((float)__ldg(a.rs + i), zi, (b0 + b1) + (b2 + b3));
+  return fmaf(rs32[i], zi, (b0 + b1) + (b2 + b3));
 }
 
-// out = M^-1 q as FP32 (hi, lo) pairs; block partial of sum(out) into slot
+// The row's A P g1 in FP32: rowsum_i g_own + sum_c (A P)_ic (g_c - g_own) from the FP32 direction
+// table and the FP32 level-1 solution g, in the pair order of k_mg_rows; the searched list (rare:
+// periodic partners, mirror parents outside the 3x3) from the FP64 pairs rounded to FP32.
+__device__ __forceinline__ float ap_stencil32(const float* __restrict__ rv9, const int* __restrict__ ragg,
+                                              const double* __restrict__ rval, int rx, size_t i, size_t n,
+                                              const float* g, int own, int ncx, float gc, float rs) {
+  const unsigned used = ((unsigned)rx >> 16) & 0xffu;
+  float v8[8], g8[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int q = k < 4 ? k : k + 1;
+    const int off = (q / 3 - 1) * ncx + (q % 3 - 1);
+    v8[k] = __ldg(rv9 + (size_t)k * n + i);
+    g8[k] = g[(used >> k) & 1u ? own + off : own];
+  }
+  float ap = rs * gc;
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+    if ((used >> k) & 1u) ap = fmaf(v8[k], g8[k] - gc, ap);
+  const int t0 = rx & 0xff, m = (rx >> 8) & 0xff;
+  for (int t = t0; t < m; ++t) {
+    const size_t e = (size_t)t * n + i;
+    ap = fmaf((float)__ldg(rval + e), g[__ldg(ragg + e)] - gc, ap);
+  }
+  return ap;
+}
+
+// out = M^-1 q in FP64 (the preconditioned direction); block partial of sum(out) into slot
 // The vector passes of this solver take two rows per thread per pass, i and i + stride (the
 // rows each thread owns stay the same), and issue all of a pass's loads before its stores: the
 // compiler cannot move a load above a store to another array it may alias.
-__device__ bool mg_vcycle_mixed(const MgMxArgs& a, double* q, double qshift, float2* out, double* slot,
+__device__ bool mg_vcycle_mixed(const MgMxArgs& a, double* q, double qshift, double* out, double* slot,
                                 double* sh, int tid, int stride) {
   const int n = a.b.n;
   Scal* s = a.b.sc;
   float* z = a.z;
-  // q -= qshift (the closed domain's mean removal), then z = omega D^-1 q
+  // q -= qshift (the closed domain's mean removal), its FP32 rounding q32, and z = omega D^-1 q
+  float* q32 = a.q32;
   for (int i = tid; i < n; i += 2 * stride) {
     const int j = i + stride;
     const bool h = j < n;
     const double qi = q[i] - qshift, qj = h ? q[j] - qshift : 0.0;
     const float di = a.dinv0[i], dj = h ? a.dinv0[j] : 0.f;
+    const float fi = (float)qi, fj = (float)qj;
     q[i] = qi;
-    z[i] = (float)MG_OMEGA * di * (float)qi;
+    q32[i] = fi;
+    z[i] = (float)MG_OMEGA * di * fi;
     if (h) {
       q[j] = qj;
-      z[j] = (float)MG_OMEGA * dj * (float)qj;
+      q32[j] = fj;
+      z[j] = (float)MG_OMEGA * dj * fj;
     }
   }
   if (!grid_sync(s)) return false;
-  for (int i = tid; i < n; i += stride) a.fr[i] = (float)q[i] - spmv_diff32s(a.b, z, i);
+  for (int i = tid; i < n; i += stride) a.fr[i] = q32[i] - spmv_diff32s(a.b, a.rs32, z, i);
   if (!grid_sync(s)) return false;
   {
     const MgLevel L1 = a.lv[0];
     for (int cc = tid; cc < L1.n; cc += stride) {
       const int s0 = __ldg(a.cstart + cc), ne = __ldg(a.ccnt + cc);
-      double b = 0.0;
+      float b32 = 0.f;  // the cell's residuals summed in FP32, in cell-list order
       for (int k = 0; k < ne; ++k) {
         const int i = __ldg(a.ip + s0 + k);
         if (i >= n) break;
-        b += (double)a.fr[i];
+        b32 += a.fr[i];
       }
+      const double b = (double)b32;
       L1.b[cc] = b;
       L1.x[cc] = MG_OMEGA * __ldg(L1.dinv + cc) * b;
     }
@@ -809,57 +944,55 @@ __device__ bool mg_vcycle_mixed(const MgMxArgs& a, double* q, double qshift, flo
   c.tail = a.tail;
   c.kinv = a.kinv;
   c.kinv_ok = a.kinv_ok;
+  c.g32 = a.g32;
   for (int l = 0; l < a.tail; ++l) {
-    const MgLevel F = a.lv[l], G = a.lv[l + 1];
-    lv_residual(F, tid, stride);
-    if (!grid_sync(s)) return false;
-    lv_restrict(F, G, tid, stride);
+    lv_residual_restrict(a.lv[l], a.lv[l + 1], tid, stride);
     if (!grid_sync(s)) return false;
   }
   if (blockIdx.x == 0) mg_block_levels(c);
   if (!grid_sync(s)) return false;
   for (int l = a.tail - 1; l >= 0; --l) {
-    const MgLevel F = a.lv[l];
-    lv_prolong(F, lv_sol(c, l + 1), a.lv[l + 1].gx, tid, stride);
-    if (!grid_sync(s)) return false;
-    lv_smooth(F, tid, stride);
+    lv_prolong_smooth(a.lv[l], lv_sol(c, l + 1), a.lv[l + 1].gx, tid, stride, l == 0 ? a.g32 : nullptr);
     if (!grid_sync(s)) return false;
   }
-  // prolongation to the particles (pre-smoothed only), output as FP32 (hi, lo) pairs, and
-  // w = A out as in the FP64 V-cycle: A z = q - fr (q as rounded to FP32 for fr), plus
-  // gamma (A P) g1 in difference form with the mixed operator's row sums
-  const double* g1 = lv_sol(c, 0);
+  // prolongation to the particles (pre-smoothed only) from the FP32 level-1 solution g, and
+  // w = A out, both in FP32 (the precision of this solver's products): A z = q32 - fr, plus
+  // gamma (A P) g in difference form with the FP32 row sums.  The output is stored as FP64 and
+  // summed in FP64 (the mean removal).  This GPU issues FP64 at 1/64 of the FP32 rate, so the
+  // pass keeps to FP32 arithmetic; streamed operands are loaded one pass ahead of the gathers.
+  const float* g32 = a.g32;
+  const float gam = (float)MG_GAMMA;
   double acc = 0.0;
-  // two rows per pass (i and i + stride), every load of both issued before the gathers
-  for (int i = tid; i < n; i += 2 * stride) {
-    const int j = i + stride;
-    const bool h = j < n;
-    const int jj = h ? j : i;  // a second row past n repeats row i's loads and stores nothing
-    const int cci = __ldg(a.agg + i), mci = __ldg(a.rcnt + i);
-    const int ccj = __ldg(a.agg + jj), mcj = __ldg(a.rcnt + jj);
-    const float zi = z[i], fri = a.fr[i], zj = z[jj], frj = a.fr[jj];
-    const double qi = q[i], rsi = __ldg(a.b.rs + i), qj = q[jj], rsj = __ldg(a.b.rs + jj);
-    const ApHead hi_ = ap_head(a.ragg, a.rval, i, n);
-    const ApHead hj_ = ap_head(a.ragg, a.rval, jj, n);
-    const double gci = g1[cci >= 0 ? cci : 0], gcj = g1[ccj >= 0 ? ccj : 0];
-    double oi = (double)zi, wi = (double)(float)qi - (double)fri;
-    double oj = (double)zj, wj = (double)(float)qj - (double)frj;
-    if (cci >= 0) {
-      oi = fma(MG_GAMMA, gci, oi);
-      wi = fma(MG_GAMMA, ap_row(hi_, a.ragg, a.rval, mci, i, n, g1, cci, gci, rsi), wi);
+  struct Row {
+    int c, rx;
+    float z, fr, rs, q;
+  };
+  auto load_row = [&](int i) {
+    Row r;
+    r.c = __ldg(a.agg + i);
+    r.rx = __ldg(a.rx + i);
+    r.z = z[i];
+    r.fr = a.fr[i];
+    r.rs = a.rs32[i];
+    r.q = q32[i];
+    return r;
+  };
+  Row cur{};
+  if (tid < n) cur = load_row(tid);
+  for (int i = tid; i < n; i += stride) {
+    const Row r = cur;
+    if (i + stride < n) cur = load_row(i + stride);
+    float oi = r.z;
+    float wi = r.q - r.fr;
+    if (r.c >= 0) {
+      const float gc = g32[r.c];
+      oi = fmaf(gam, gc, oi);
+      wi = fmaf(gam, ap_stencil32(a.rv9, a.ragg, a.rval, r.rx, i, n, g32, r.c, a.ncx, gc, r.rs), wi);
     }
-    if (ccj >= 0) {
-      oj = fma(MG_GAMMA, gcj, oj);
-      wj = fma(MG_GAMMA, ap_row(hj_, a.ragg, a.rval, mcj, jj, n, g1, ccj, gcj, rsj), wj);
-    }
-    out[i] = split2(oi);
+    const double od = (double)oi;
+    out[i] = od;
     a.w[i] = wi;
-    acc += oi;
-    if (h) {
-      out[j] = split2(oj);
-      a.w[j] = wj;
-      acc += oj;
-    }
+    acc += od;
   }
   write_partials(acc, 0.0, 1, slot, sh);
   return true;
@@ -880,11 +1013,15 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
   double* part = a.part;
   const double rinv1 = 1.0 / (1.0 + 1.0e-15);
   const double small = NONULL ? 1.0e-6 : 4.0;
-  double red[2];
+  double red[4];
   double acc = 0.0;
   // out = M^-1 (q - qshift), with q -= qshift stored back; block partial of sum(out) into slot
+  // With the multigrid the preconditioned directions are FP64 (pi, si read as double: same
+  // size as the (hi, lo) pairs the unpreconditioned products gather)
+  double* const pd = reinterpret_cast<double*>(a.pi);
+  double* const sd = reinterpret_cast<double*>(a.si);
   auto precond = [&](double* q, double qshift, float2* out, double* slot) -> bool {
-    if (use_mg) return mg_vcycle_mixed(m, q, qshift, out, slot, sh, tid, stride);
+    if (use_mg) return mg_vcycle_mixed(m, q, qshift, reinterpret_cast<double*>(out), slot, sh, tid, stride);
     double sum = 0.0;
     for (int i = tid; i < n; i += stride) {
       const double qi = q[i] - qshift;
@@ -898,10 +1035,12 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
   };
   for (int i = tid; i < n; i += stride) {
     // 1/diag from the row sum and the FP32 off-diagonal values (diag = rowsum - sum_k A_ik)
-    double dg = __ldg(a.rs + i);
+    const double rsi = __ldg(a.rs + i);
+    double dg = rsi;
     const int cnt = __ldg(a.cnt + i);
     for (int k = 0; k < cnt; ++k) dg -= (double)__ldg(a.val32 + (size_t)k * a.stride + i);
     m.dinv0[i] = dg != 0.0 ? (float)(1.0 / dg) : 0.f;
+    m.rs32[i] = (float)rsi;
   }
   if (a.warm) {
     for (int i = tid; i < n; i += stride) {
@@ -924,13 +1063,14 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
   write_partials(acc, 0.0, 1, part + 10 * (size_t)nb, sh);
   if (!grid_sync(s)) return;
   reduce_partials(part + 10 * (size_t)nb, nb, 1, red, shv);
-  double rho = red[0], rho0 = 1.0, alpha = 1.0, omega = 1.0;
+  double rho = red[0], alpha = 1.0, omega = 1.0;
+  double beta = 0.0;  // for iteration 2 on, derived with the previous iteration's last reduction
+  const double dn = (double)n;
   double n2r0 = 1.0, n2s0 = 1.0, resid = 0.0;
   int iter = 1, warn = 0;
   bool done = false;
   while (iter <= a.itermax) {
     if (rho == 0.0) { warn |= VEBI_WARN_BICGSTAB_BREAKDOWN; done = true; break; }
-    const double beta = rho / (rho0 + 1.0e-15) * alpha / (omega + 1.0e-15);
     acc = 0.0;
     for (int i = tid; i < n; i += 2 * stride) {
       const int j = i + stride;
@@ -950,20 +1090,20 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
     if (NONULL) {
       write_partials(acc, 0.0, 1, part, sh);
       if (!grid_sync(s)) return;
-      reduce_partials(part, nb, 1, red, shv);
-      mean = red[0] / (double)n;
+      reduce_partials(part, nb, 1, red, shv, [=](double* v) { v[0] = v[0] / dn; });
+      mean = red[0];
     }
     if (!precond(a.p, mean, a.pi, part + 1 * (size_t)nb)) return;
     if (!grid_sync(s)) return;
-    reduce_partials(part + 1 * (size_t)nb, nb, 1, red, shv);
-    const double mp = NONULL ? red[0] / (double)n : 0.0;
+    reduce_partials(part + 1 * (size_t)nb, nb, 1, red, shv, [=](double* v) { v[0] = NONULL ? v[0] / dn : 0.0; });
+    const double mp = red[0];
     acc = 0.0;
     if (use_mg) {
       for (int i = tid; i < n; i += 2 * stride) {
         const int j = i + stride;
         const bool h = j < n;
-        const double wi = m.w[i], rsi = __ldg(a.rs + i), rbi = a.rb[i];
-        const double wj = h ? m.w[j] : 0.0, rsj = h ? __ldg(a.rs + j) : 0.0, rbj = h ? a.rb[j] : 0.0;
+        const double wi = (double)m.w[i], rsi = __ldg(a.rs + i), rbi = a.rb[i];
+        const double wj = h ? (double)m.w[j] : 0.0, rsj = h ? __ldg(a.rs + j) : 0.0, rbj = h ? a.rb[j] : 0.0;
         const double vi = fma(-mp, rsi, wi);
         a.v[i] = vi;
         acc = fma(rbi, vi, acc);
@@ -982,8 +1122,8 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
     }
     write_partials(acc, 0.0, 1, part + 2 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
-    reduce_partials(part + 2 * (size_t)nb, nb, 1, red, shv);
-    alpha = rho / (red[0] + 1.0e-15);
+    reduce_partials(part + 2 * (size_t)nb, nb, 1, red, shv, [=](double* v) { v[0] = rho / (v[0] + 1.0e-15); });
+    alpha = red[0];
     double a2 = 0.0;
     acc = 0.0;
     for (int i = tid; i < n; i += 2 * stride) {
@@ -1004,28 +1144,29 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
     }
     write_partials(acc, a2, 2, part + 4 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
-    reduce_partials(part + 4 * (size_t)nb, nb, 2, red, shv);
+    reduce_partials(part + 4 * (size_t)nb, nb, 2, red, shv, [=](double* v) { v[1] = v[1] / dn; });
     const double n2s = red[0];
-    const double mean_s = red[1] / (double)n;
+    const double mean_s = red[1];
     if (iter == 1) n2s0 = (n2s <= small) ? 1.0 : n2s;
     if (n2s <= a.tol * a.tol * n2s0) {
-      for (int i = tid; i < n; i += stride) a.x[i] = fma(alpha, join2(a.pi[i]) - mp, a.x[i]);
+      for (int i = tid; i < n; i += stride)
+        a.x[i] = fma(alpha, (use_mg ? pd[i] : join2(a.pi[i])) - mp, a.x[i]);
       resid = sqrt(n2s / n2s0);
       done = true;
       break;
     }
     if (!precond(a.s, NONULL ? mean_s : 0.0, a.si, part + 3 * (size_t)nb)) return;
     if (!grid_sync(s)) return;
-    reduce_partials(part + 3 * (size_t)nb, nb, 1, red, shv);
-    const double ms = NONULL ? red[0] / (double)n : 0.0;
+    reduce_partials(part + 3 * (size_t)nb, nb, 1, red, shv, [=](double* v) { v[0] = NONULL ? v[0] / dn : 0.0; });
+    const double ms = red[0];
     acc = 0.0;
     a2 = 0.0;
     if (use_mg) {
       for (int i = tid; i < n; i += 2 * stride) {
         const int j = i + stride;
         const bool h = j < n;
-        const double wi = m.w[i], rsi = __ldg(a.rs + i), si = a.s[i];
-        const double wj = h ? m.w[j] : 0.0, rsj = h ? __ldg(a.rs + j) : 0.0, sj = h ? a.s[j] : 0.0;
+        const double wi = (double)m.w[i], rsi = __ldg(a.rs + i), si = a.s[i];
+        const double wj = h ? (double)m.w[j] : 0.0, rsj = h ? __ldg(a.rs + j) : 0.0, sj = h ? a.s[j] : 0.0;
         const double ti = fma(-ms, rsi, wi);
         a.t[i] = ti;
         acc = fma(ti, si, acc);
@@ -1047,24 +1188,37 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
     }
     write_partials(acc, a2, 2, part + 6 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
-    reduce_partials(part + 6 * (size_t)nb, nb, 2, red, shv);
-    omega = red[0] / (red[1] + 1.0e-15);
+    reduce_partials(part + 6 * (size_t)nb, nb, 2, red, shv, [](double* v) { v[0] = v[0] / (v[1] + 1.0e-15); });
+    omega = red[0];
     acc = 0.0;
     a2 = 0.0;
+    // x += alpha (p_hat - mp) + omega (s_hat - ms), with the two mean shifts folded into one
+    const double xshift = fma(alpha, mp, omega * ms);
+    // the preconditioned directions as FP64 (multigrid) or (hi, lo) pairs
+    auto dirs = [&](int i, double& pv, double& sv) {
+      if (use_mg) {
+        pv = pd[i];
+        sv = sd[i];
+      } else {
+        pv = join2(a.pi[i]);
+        sv = join2(a.si[i]);
+      }
+    };
     for (int i = tid; i < n; i += 2 * stride) {
       const int j = i + stride;
       const bool h = j < n;
-      const float2 sii = a.si[i], pii = a.pi[i];
+      double pii, sii, pij = 0.0, sij = 0.0;
+      dirs(i, pii, sii);
       const double xi = a.x[i], ti = a.t[i], s_i = a.s[i], rbi = a.rb[i];
-      const float2 sij = h ? a.si[j] : make_float2(0.f, 0.f), pij = h ? a.pi[j] : make_float2(0.f, 0.f);
+      if (h) dirs(j, pij, sij);
       const double xj = h ? a.x[j] : 0.0, tj = h ? a.t[j] : 0.0, s_j = h ? a.s[j] : 0.0, rbj = h ? a.rb[j] : 0.0;
-      a.x[i] = fma(omega, join2(sii) - ms, fma(alpha, join2(pii) - mp, xi));
+      a.x[i] = fma(omega, sii, fma(alpha, pii, xi - xshift));
       const double ri = fma(-omega, ti, s_i);
       a.r[i] = ri;
       acc = fma(ri, ri, acc);
       a2 = fma(rbi, ri, a2);
       if (h) {
-        a.x[j] = fma(omega, join2(sij) - ms, fma(alpha, join2(pij) - mp, xj));
+        a.x[j] = fma(omega, sij, fma(alpha, pij, xj - xshift));
         const double rj = fma(-omega, tj, s_j);
         a.r[j] = rj;
         acc = fma(rj, rj, acc);
@@ -1073,14 +1227,19 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
     }
     write_partials(acc, a2, 2, part + 8 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
-    reduce_partials(part + 8 * (size_t)nb, nb, 2, red, shv);
+    // v[2] = the relative residual, v[3] = the next iteration's beta from the new rho v[1]
+    reduce_partials(part + 8 * (size_t)nb, nb, 2, red, shv, [=](double* v) {
+      const double r0 = iter == 1 ? ((v[0] <= small) ? 1.0 : v[0]) : n2r0;
+      v[2] = sqrt(v[0] / r0);
+      v[3] = v[1] / (rho + 1.0e-15) * alpha / (omega + 1.0e-15);
+    });
     const double n2r = red[0];
     if (iter == 1) n2r0 = (n2r <= small) ? 1.0 : n2r;
-    resid = sqrt(n2r / n2r0);
+    resid = red[2];
     if (n2r <= a.tol * a.tol * n2r0) { done = true; break; }
     iter = iter + 1;
-    rho0 = rho;
     rho = red[1];
+    beta = red[3];
   }
   if (!done) warn |= VEBI_WARN_MAXITER;
   for (int i = tid; i < n; i += stride) a.P[i] = a.x[i];
@@ -1123,7 +1282,8 @@ static int mg_setup(Ctx& x) {
   const Consts& c = x.c;
   const int nl = (int)x.mg.size();
   const float* v32 = x.precision == VEBI_PREC_MIXED ? x.d.ppe_val32 : nullptr;
-  VEBI_LAUNCH(x, k_mg_rows, grid_for(c.npfb), TPB, c, x.d, v32, x.mg_ragg, x.mg_rval, x.mg_rcnt);
+  VEBI_LAUNCH(x, k_mg_rows, grid_for(c.npfb), TPB, c, x.d, v32, x.mg_ragg, x.mg_rval, x.mg_rcnt, x.mg_rv9,
+              x.mg_rx);
   VEBI_LAUNCH(x, k_mg_level1, grid_for(x.mg[0].n), TPB, c, x.d, x.mg[0], x.mg_ragg, x.mg_rval, x.mg_rcnt);
   for (int l = 0; l + 1 < nl; ++l)
     VEBI_LAUNCH(x, k_mg_coarsen, grid_for(x.mg[l + 1].n), TPB, x.mg[l], x.mg[l + 1], x.d.s);
@@ -1156,8 +1316,8 @@ void launch_ppe_mg_mixed(Ctx& x) {
                     d.rowsum, d.ppe_val32, d.ppe_col, d.ij_count, d.s, (long long)c.npfb, c.npfb, c.itermax, c.tol,
                     c.warm_start},
              x.d_mg, (int)x.mg.size(), tail, d.cellpart, d.cell_start, d.cell_cnt, d.ip, (float*)x.mg_z,
-             (float*)x.mg_fr, (float*)x.mg_dinv0, x.mg_ragg, x.mg_rcnt, x.mg_rval, x.mg_w, x.mg_kinv,
-             x.mg_kinv_ok};
+             (float*)x.mg_fr, (float*)x.mg_dinv0, x.mg_ragg, x.mg_rx, x.mg_rval, (const float*)x.mg_rv9, c.ncx,
+             (float*)x.mg_w, x.mg_kinv, x.mg_kinv_ok, x.mg_g32, (float*)x.mg_rsum, x.mg_q32};
   if (c.open_domain == 0) cudaLaunchKernelEx(&cfg, k_bicgstab_mixed_mg<true>, m);
   else cudaLaunchKernelEx(&cfg, k_bicgstab_mixed_mg<false>, m);
   x.launches++;
@@ -1185,7 +1345,7 @@ void launch_ppe_mg(Ctx& x) {
                   d.ppe_diag, d.ppe_val, d.ppe_col, d.ij_count, d.s, (long long)c.npfb, c.npfb, c.itermax, c.tol,
                   c.warm_start},
            x.d_mg, nl, tail, d.cellpart, d.cell_start, d.cell_cnt, d.ip, x.mg_z, x.mg_fr, x.mg_dinv0, x.mg_rsum,
-           x.mg_ragg, x.mg_rcnt, x.mg_rval, x.mg_w, x.mg_kinv, x.mg_kinv_ok};
+           x.mg_ragg, x.mg_rx, x.mg_rval, x.mg_rv9, c.ncx, x.mg_w, x.mg_kinv, x.mg_kinv_ok};
   if (c.open_domain == 0) cudaLaunchKernelEx(&cfg, k_bicgstab_mg<true>, m);
   else cudaLaunchKernelEx(&cfg, k_bicgstab_mg<false>, m);
   x.launches++;
@@ -1197,7 +1357,18 @@ void launch_ppe_mg(Ctx& x) {
 // diagnostic build only: the multigrid solvers' barrier timestamps (see vebi_solver.cuh)
 extern "C" int vebi_barrier_timestamps_reset(void) {
   unsigned int z = 0;
-  return (int)cudaMemcpyToSymbol(vebi::g_bar_n, &z, sizeof(z));
+  static unsigned int zb[vebi::BAR_ALL_BLOCKS];
+  cudaError_t e = cudaMemcpyToSymbol(vebi::g_bar_blk_n, zb, sizeof(zb));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(vebi::g_bar_n, &z, sizeof(z));
+  return (int)e;
+}
+// every block's arrival at BAR_ALL_N barriers from BAR_ALL_FIRST on ([q][block]), and its SM
+extern "C" int vebi_barrier_arrivals_read(unsigned long long* arr, unsigned int* smid) {
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess)
+    e = cudaMemcpyFromSymbol(arr, vebi::g_bar_all, sizeof(unsigned long long) * vebi::BAR_ALL_N * vebi::BAR_ALL_BLOCKS);
+  if (e == cudaSuccess) e = cudaMemcpyFromSymbol(smid, vebi::g_bar_smid, sizeof(unsigned int) * vebi::BAR_ALL_BLOCKS);
+  return (int)e;
 }
 extern "C" int vebi_barrier_timestamps_read(unsigned long long* ts, unsigned int* n) {
   cudaError_t e = cudaDeviceSynchronize();

@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(TPB) k_na_bicgstab(NaArgs a) {
   double* x = a.x;
   const double small = NONULL ? 1.0e-6 : 4.0;
   auto den = [&](int i) -> double { return NONULL ? (1.0 + 1.0e-15) : (a.diag[i] + 1.0e-15); };
-  double red[2];
+  double red[4];
   double acc = 0.0;
   for (int i = tid; i < n; i += stride) {
     double bi = a.rhs[i];

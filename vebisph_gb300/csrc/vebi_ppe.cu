@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
   double* part = a.part;
   const double rinv1 = 1.0 / (1.0 + 1.0e-15);
   const double small = NONULL ? 1.0e-6 : 4.0;  // open solver: the integer expression 10-6
-  double red[2];
+  double red[4];
   double acc = 0.0;
   if (a.warm) {  // x0 = P of the previous step: r0 = B - A x0 (the SpMV reads x through pinv)
     for (int i = tid; i < n; i += stride) {
@@ -170,16 +170,17 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
   write_partials(acc, 0.0, 1, part + 10 * (size_t)nb, sh);
   if (!grid_sync(s)) return;
   reduce_partials(part + 10 * (size_t)nb, nb, 1, red, shv);
-  double rho = red[0], rho0 = 1.0, alpha = 1.0, omega = 1.0;
+  double rho = red[0], alpha = 1.0, omega = 1.0;
   double n2r0 = 1.0, n2s0 = 1.0, resid = 0.0;
+  double beta = 0.0;  // for iteration 2 on, derived with the previous iteration's last reduction
   int iter = 1, warn = 0;
   bool done = false;
+  const double dn = (double)n;
   while (iter <= a.itermax) {
     if (rho == 0.0) { warn |= VEBI_WARN_BICGSTAB_BREAKDOWN; done = true; break; }
     // p = r + beta (p - omega v).  The vector passes take rows i and i + stride per thread (the
     // rows a thread owns do not change) and issue their loads before their stores: the compiler
     // cannot move a load of one array above a store to another that may alias it.
-    const double beta = rho / (rho0 + 1.0e-15) * alpha / (omega + 1.0e-15);
     acc = 0.0;
     for (int i = tid; i < n; i += 2 * stride) {
       const int j = i + stride;
@@ -199,8 +200,8 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
     if (NONULL) {
       write_partials(acc, 0.0, 1, slot, sh);
       if (!grid_sync(s)) return;
-      reduce_partials(slot, nb, 1, red, shv);
-      const double mean = red[0] / (double)n;
+      reduce_partials(slot, nb, 1, red, shv, [=](double* v) { v[0] = v[0] / dn; });
+      const double mean = red[0];
       for (int i = tid; i < n; i += stride) {
         double pi = a.p[i] - mean;
         a.p[i] = pi;
@@ -220,8 +221,8 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
     slot = part + 2 * (size_t)nb;
     write_partials(acc, 0.0, 1, slot, sh);
     if (!grid_sync(s)) return;
-    reduce_partials(slot, nb, 1, red, shv);
-    alpha = rho / (red[0] + 1.0e-15);
+    reduce_partials(slot, nb, 1, red, shv, [=](double* v) { v[0] = rho / (v[0] + 1.0e-15); });
+    alpha = red[0];
     // s = r - alpha v ; |s|^2 ; sum(s)
     double a2 = 0.0;
     acc = 0.0;
@@ -244,9 +245,9 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
     slot = part + 4 * (size_t)nb;
     write_partials(acc, a2, 2, slot, sh);
     if (!grid_sync(s)) return;
-    reduce_partials(slot, nb, 2, red, shv);
+    reduce_partials(slot, nb, 2, red, shv, [=](double* v) { v[1] = v[1] / dn; });
     const double n2s = red[0];
-    const double mean_s = red[1] / (double)n;
+    const double mean_s = red[1];
     if (iter == 1) n2s0 = (n2s <= small) ? 1.0 : n2s;
     if (n2s <= a.tol * a.tol * n2s0) {
       for (int i = tid; i < n; i += stride) a.x[i] = fma(alpha, a.pinv[i], a.x[i]);
@@ -273,8 +274,8 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
     slot = part + 6 * (size_t)nb;
     write_partials(acc, a2, 2, slot, sh);
     if (!grid_sync(s)) return;
-    reduce_partials(slot, nb, 2, red, shv);
-    omega = red[0] / (red[1] + 1.0e-15);
+    reduce_partials(slot, nb, 2, red, shv, [](double* v) { v[0] = v[0] / (v[1] + 1.0e-15); });
+    omega = red[0];
     // x, r update ; |r|^2 ; (r_bar, r) for the next rho
     acc = 0.0;
     a2 = 0.0;
@@ -300,14 +301,19 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
     slot = part + 8 * (size_t)nb;
     write_partials(acc, a2, 2, slot, sh);
     if (!grid_sync(s)) return;
-    reduce_partials(slot, nb, 2, red, shv);
+    // v[2] = the relative residual, v[3] = the next iteration's beta from the new rho v[1]
+    reduce_partials(slot, nb, 2, red, shv, [=](double* v) {
+      const double r0 = iter == 1 ? ((v[0] <= small) ? 1.0 : v[0]) : n2r0;
+      v[2] = sqrt(v[0] / r0);
+      v[3] = v[1] / (rho + 1.0e-15) * alpha / (omega + 1.0e-15);
+    });
     const double n2r = red[0];
     if (iter == 1) n2r0 = (n2r <= small) ? 1.0 : n2r;
-    resid = sqrt(n2r / n2r0);
+    resid = red[2];
     if (n2r <= a.tol * a.tol * n2r0) { done = true; break; }
     iter = iter + 1;
-    rho0 = rho;
     rho = red[1];
+    beta = red[3];
   }
   if (!done) warn |= VEBI_WARN_MAXITER;
   for (int i = tid; i < n; i += stride) a.P[i] = a.x[i];
@@ -432,7 +438,7 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab_mixed(MxArgs a) {
   double* part = a.part;
   const double rinv1 = 1.0 / (1.0 + 1.0e-15);
   const double small = NONULL ? 1.0e-6 : 4.0;
-  double red[2];
+  double red[4];
   double acc = 0.0;
   if (a.warm) {  // x0 = P of the previous step
     for (int i = tid; i < n; i += stride) {
@@ -455,13 +461,14 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab_mixed(MxArgs a) {
   write_partials(acc, 0.0, 1, part + 10 * (size_t)nb, sh);
   if (!grid_sync(s)) return;
   reduce_partials(part + 10 * (size_t)nb, nb, 1, red, shv);
-  double rho = red[0], rho0 = 1.0, alpha = 1.0, omega = 1.0;
+  double rho = red[0], alpha = 1.0, omega = 1.0;
   double n2r0 = 1.0, n2s0 = 1.0, resid = 0.0;
+  double beta = 0.0;  // for iteration 2 on, derived with the previous iteration's last reduction
   int iter = 1, warn = 0;
   bool done = false;
+  const double dn = (double)n;
   while (iter <= a.itermax) {
     if (rho == 0.0) { warn |= VEBI_WARN_BICGSTAB_BREAKDOWN; done = true; break; }
-    const double beta = rho / (rho0 + 1.0e-15) * alpha / (omega + 1.0e-15);
     acc = 0.0;
     for (int i = tid; i < n; i += stride) {
       double pi = (iter == 1) ? a.r[i] : fma(beta, fma(-omega, a.v[i], a.p[i]), a.r[i]);
@@ -472,8 +479,8 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab_mixed(MxArgs a) {
     if (NONULL) {
       write_partials(acc, 0.0, 1, part, sh);
       if (!grid_sync(s)) return;
-      reduce_partials(part, nb, 1, red, shv);
-      mean = red[0] / (double)n;
+      reduce_partials(part, nb, 1, red, shv, [=](double* v) { v[0] = v[0] / dn; });
+      mean = red[0];
     }
     for (int i = tid; i < n; i += stride) {
       double pi = a.p[i];
@@ -489,8 +496,8 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab_mixed(MxArgs a) {
     }
     write_partials(acc, 0.0, 1, part + 2 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
-    reduce_partials(part + 2 * (size_t)nb, nb, 1, red, shv);
-    alpha = rho / (red[0] + 1.0e-15);
+    reduce_partials(part + 2 * (size_t)nb, nb, 1, red, shv, [=](double* v) { v[0] = rho / (v[0] + 1.0e-15); });
+    alpha = red[0];
     double a2 = 0.0;
     acc = 0.0;
     for (int i = tid; i < n; i += stride) {
@@ -501,9 +508,9 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab_mixed(MxArgs a) {
     }
     write_partials(acc, a2, 2, part + 4 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
-    reduce_partials(part + 4 * (size_t)nb, nb, 2, red, shv);
+    reduce_partials(part + 4 * (size_t)nb, nb, 2, red, shv, [=](double* v) { v[1] = v[1] / dn; });
     const double n2s = red[0];
-    const double mean_s = red[1] / (double)n;
+    const double mean_s = red[1];
     if (iter == 1) n2s0 = (n2s <= small) ? 1.0 : n2s;
     if (n2s <= a.tol * a.tol * n2s0) {
       for (int i = tid; i < n; i += stride) a.x[i] = fma(alpha, join2(a.pi[i]), a.x[i]);
@@ -527,8 +534,8 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab_mixed(MxArgs a) {
     }
     write_partials(acc, a2, 2, part + 6 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
-    reduce_partials(part + 6 * (size_t)nb, nb, 2, red, shv);
-    omega = red[0] / (red[1] + 1.0e-15);
+    reduce_partials(part + 6 * (size_t)nb, nb, 2, red, shv, [](double* v) { v[0] = v[0] / (v[1] + 1.0e-15); });
+    omega = red[0];
     acc = 0.0;
     a2 = 0.0;
     for (int i = tid; i < n; i += stride) {
@@ -540,14 +547,19 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab_mixed(MxArgs a) {
     }
     write_partials(acc, a2, 2, part + 8 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
-    reduce_partials(part + 8 * (size_t)nb, nb, 2, red, shv);
+    // v[2] = the relative residual, v[3] = the next iteration's beta from the new rho v[1]
+    reduce_partials(part + 8 * (size_t)nb, nb, 2, red, shv, [=](double* v) {
+      const double r0 = iter == 1 ? ((v[0] <= small) ? 1.0 : v[0]) : n2r0;
+      v[2] = sqrt(v[0] / r0);
+      v[3] = v[1] / (rho + 1.0e-15) * alpha / (omega + 1.0e-15);
+    });
     const double n2r = red[0];
     if (iter == 1) n2r0 = (n2r <= small) ? 1.0 : n2r;
-    resid = sqrt(n2r / n2r0);
+    resid = red[2];
     if (n2r <= a.tol * a.tol * n2r0) { done = true; break; }
     iter = iter + 1;
-    rho0 = rho;
     rho = red[1];
+    beta = red[3];
   }
   if (!done) warn |= VEBI_WARN_MAXITER;
   for (int i = tid; i < n; i += stride) a.P[i] = a.x[i];

@@ -16,6 +16,12 @@ constexpr unsigned long long SPIN_LIMIT = 1ull << 25;  // ~2-4 s of __nanosleep(
 constexpr int BAR_TS_MAX = 16384;
 static __device__ unsigned long long g_bar_ts[2][BAR_TS_MAX];
 static __device__ unsigned int g_bar_n;
+// every block's arrival time at the barriers BAR_ALL_FIRST .. BAR_ALL_FIRST + BAR_ALL_N - 1 of
+// the solve (one iteration and more), and the SM each block runs on
+constexpr int BAR_ALL_FIRST = 200, BAR_ALL_N = 64, BAR_ALL_BLOCKS = 2048;
+static __device__ unsigned int g_bar_blk_n[BAR_ALL_BLOCKS];
+static __device__ unsigned long long g_bar_all[BAR_ALL_N][BAR_ALL_BLOCKS];
+static __device__ unsigned int g_bar_smid[BAR_ALL_BLOCKS];
 __device__ __forceinline__ unsigned long long bar_clock() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -63,15 +69,31 @@ __device__ __forceinline__ bool grid_sync_bounded(Scal* s, unsigned long long li
       g_bar_ts[1][q] = bar_clock();
     }
   }
+  if (threadIdx.x == 0 && blockIdx.x < BAR_ALL_BLOCKS) {
+    const unsigned int q = g_bar_blk_n[blockIdx.x]++;
+    if (q >= BAR_ALL_FIRST && q < BAR_ALL_FIRST + BAR_ALL_N) g_bar_all[q - BAR_ALL_FIRST][blockIdx.x] = ts_arrive;
+    if (q == 0) {
+      unsigned int sm;
+      asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
+      g_bar_smid[blockIdx.x] = sm;
+    }
+  }
 #endif
   return *((volatile int*)&s->error) == 0;
 }
 
 __device__ __forceinline__ bool grid_sync(Scal* s) { return grid_sync_bounded(s, SPIN_LIMIT); }
 
-// sum of the block partials of `slot` in a fixed order; identical in every block
-__device__ __forceinline__ void reduce_partials(const double* part, int nb, int nval, double* out,
-                                                double* shv) {
+// Sum of the block partials of `slot` in a fixed order; identical in every block.  `post`,
+// run by thread 0 alone on the nval sums in v[0..3] before they are shared, derives the
+// iteration's scalars (its divisions and square roots) in place: this GPU issues FP64 at 1/64
+// of the FP32 rate, so uniform FP64 work is done once per block rather than once per warp.
+struct NoPost {
+  __device__ void operator()(double*) const {}
+};
+template <class Post = NoPost>
+__device__ __forceinline__ void reduce_partials(const double* part, int nb, int nval, double* out, double* shv,
+                                                Post post = Post()) {
   if (threadIdx.x < 32) {
     for (int q = 0; q < nval; ++q) {
       double v = 0.0;
@@ -79,9 +101,10 @@ __device__ __forceinline__ void reduce_partials(const double* part, int nb, int 
       for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
       if (threadIdx.x == 0) shv[q] = v;
     }
+    if (threadIdx.x == 0) post(shv);
   }
   __syncthreads();
-  for (int q = 0; q < nval; ++q) out[q] = shv[q];
+  for (int q = 0; q < 4; ++q) out[q] = shv[q];
   __syncthreads();
 }
 
@@ -89,14 +112,17 @@ __device__ __forceinline__ void reduce_partials(const double* part, int nb, int 
 __device__ __forceinline__ void write_partials(double a, double b, int nval, double* part, double* sh) {
   for (int o = 16; o > 0; o >>= 1) {
     a += __shfl_down_sync(0xffffffffu, a, o);
-    b += __shfl_down_sync(0xffffffffu, b, o);
+    if (nval > 1) b += __shfl_down_sync(0xffffffffu, b, o);
   }
   int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   if (l == 0) { sh[w] = a; sh[32 + w] = b; }
   __syncthreads();
   if (threadIdx.x == 0) {
     double sa = 0.0, sb = 0.0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { sa += sh[q]; sb += sh[32 + q]; }
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+      sa += sh[q];
+      if (nval > 1) sb += sh[32 + q];
+    }
     part[blockIdx.x] = sa;
     if (nval > 1) part[gridDim.x + blockIdx.x] = sb;
   }
