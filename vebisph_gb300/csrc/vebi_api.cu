@@ -13,7 +13,7 @@ namespace vebi {
 
 int ppe_solver_blocks(int device, int nsm);
 int ppe_mixed_blocks(int nsm);
-int ppe_mg_blocks(int nsm);
+int ppe_mg_blocks(int nsm, bool mixed);
 std::vector<int> mg_level_dims(int gx, int gy);
 void dump_free(Ctx& x);
 int dump_async(Ctx& x);
@@ -249,6 +249,7 @@ static int allocate_all(Ctx& x) {
   int part_blocks = x.coop_blocks;
   if (x.coop_blocks_mixed > part_blocks) part_blocks = x.coop_blocks_mixed;
   if (x.mg_blocks > part_blocks) part_blocks = x.mg_blocks;
+  if (x.mg_blocks_mixed > part_blocks) part_blocks = x.mg_blocks_mixed;
   size_t coop_part = (size_t)part_blocks * 12;
   A_(d.partials, (2 * np_part > coop_part ? 2 * np_part : coop_part) + 64);
   A_(d.gpx, n); A_(d.gpy, n);
@@ -323,7 +324,8 @@ int vebi_create(const vebi_params* params, vebi_ctx** out) {
   x.coop_blocks = ppe_solver_blocks(x.device, x.nsm);
   x.coop_blocks_mixed = ppe_mixed_blocks(x.nsm);
   x.gs_blocks = x.nsm * 8;
-  x.mg_blocks = ppe_mg_blocks(x.nsm);
+  x.mg_blocks = ppe_mg_blocks(x.nsm, false);
+  x.mg_blocks_mixed = ppe_mg_blocks(x.nsm, true);
   if (cudaStreamCreateWithFlags(&x.st, cudaStreamNonBlocking) != cudaSuccess) {
     delete h;
     return fail(VEBI_ERR_CUDA, "cudaStreamCreate failed");

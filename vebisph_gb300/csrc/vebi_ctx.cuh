@@ -41,7 +41,8 @@ struct Ctx {
   // multigrid-preconditioned PPE (opt-in)
   std::vector<MgLevel> mg;         // coarse levels, finest first
   MgLevel* d_mg = nullptr;         // device copy of the level descriptors
-  int mg_blocks = 0;               // co-resident blocks of the preconditioned solver
+  int mg_blocks = 0;               // co-resident blocks of the preconditioned solver (FP64)
+  int mg_blocks_mixed = 0;         // the same for the mixed-precision kernel
   double *mg_z = nullptr, *mg_fr = nullptr, *mg_dinv0 = nullptr, *mg_rsum = nullptr, *mg_w = nullptr;
   int *mg_ragg = nullptr, *mg_rcnt = nullptr;  // per-row (cell, value) pairs of the level-1 build
   double* mg_kinv = nullptr;       // dense inverse of the coarsest level

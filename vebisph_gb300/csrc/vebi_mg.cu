@@ -904,21 +904,19 @@ __device__ bool mg_vcycle_mixed(const MgMxArgs& a, double* q, double qshift, dou
   float* z = a.z;
   // q -= qshift (the closed domain's mean removal), its FP32 rounding q32, and z = omega D^-1 q
   float* q32 = a.q32;
-  for (int i = tid; i < n; i += 2 * stride) {
-    const int j = i + stride;
-    const bool h = j < n;
-    const double qi = q[i] - qshift, qj = h ? q[j] - qshift : 0.0;
-    const float di = a.dinv0[i], dj = h ? a.dinv0[j] : 0.f;
-    const float fi = (float)qi, fj = (float)qj;
-    q[i] = qi;
-    q32[i] = fi;
-    z[i] = (float)MG_OMEGA * di * fi;
-    if (h) {
-      q[j] = qj;
-      q32[j] = fj;
-      z[j] = (float)MG_OMEGA * dj * fj;
-    }
-  }
+  struct QRow {
+    double q;
+    float d;
+  };
+  rows_ahead(
+      tid, stride, n, [&](int i) { return QRow{q[i], a.dinv0[i]}; },
+      [&](int i, const QRow& o) {
+        const double qi = o.q - qshift;
+        const float fi = (float)qi;
+        q[i] = qi;
+        q32[i] = fi;
+        z[i] = (float)MG_OMEGA * o.d * fi;
+      });
   if (!grid_sync(s)) return false;
   for (int i = tid; i < n; i += stride) a.fr[i] = q32[i] - spmv_diff32s(a.b, a.rs32, z, i);
   if (!grid_sync(s)) return false;
@@ -998,8 +996,13 @@ __device__ bool mg_vcycle_mixed(const MgMxArgs& a, double* q, double qshift, dou
   return true;
 }
 
+// Blocks per SM the mixed kernel is compiled for: its register budget is 65536 / (TPB x this)
+#ifndef VEBI_MIXED_MG_BLOCKS_PER_SM
+#define VEBI_MIXED_MG_BLOCKS_PER_SM 4
+#endif
+
 template <bool NONULL>
-__global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
+__global__ void __launch_bounds__(TPB, VEBI_MIXED_MG_BLOCKS_PER_SM) k_bicgstab_mixed_mg(MgMxArgs m) {
   __shared__ double sh[64];
   __shared__ double shv[4];
   const MxArgs& a = m.b;
@@ -1072,20 +1075,14 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
   while (iter <= a.itermax) {
     if (rho == 0.0) { warn |= VEBI_WARN_BICGSTAB_BREAKDOWN; done = true; break; }
     acc = 0.0;
-    for (int i = tid; i < n; i += 2 * stride) {
-      const int j = i + stride;
-      const bool h = j < n;
-      const double ri = a.r[i], vi = a.v[i], pi = a.p[i];
-      const double rj = h ? a.r[j] : 0.0, vj = h ? a.v[j] : 0.0, pj = h ? a.p[j] : 0.0;
-      const double ni = (iter == 1) ? ri : fma(beta, fma(-omega, vi, pi), ri);
-      a.p[i] = ni;
-      acc += ni;
-      if (h) {
-        const double nj = (iter == 1) ? rj : fma(beta, fma(-omega, vj, pj), rj);
-        a.p[j] = nj;
-        acc += nj;
-      }
-    }
+    // The vector passes load each row's operands one row ahead (rows_ahead)
+    rows_ahead(
+        tid, stride, n, [&](int i) { return make_double3(a.r[i], a.v[i], a.p[i]); },
+        [&](int i, const double3& o) {
+          const double ni = (iter == 1) ? o.x : fma(beta, fma(-omega, o.y, o.z), o.x);
+          a.p[i] = ni;
+          acc += ni;
+        });
     double mean = 0.0;
     if (NONULL) {
       write_partials(acc, 0.0, 1, part, sh);
@@ -1099,20 +1096,13 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
     const double mp = red[0];
     acc = 0.0;
     if (use_mg) {
-      for (int i = tid; i < n; i += 2 * stride) {
-        const int j = i + stride;
-        const bool h = j < n;
-        const double wi = (double)m.w[i], rsi = __ldg(a.rs + i), rbi = a.rb[i];
-        const double wj = h ? (double)m.w[j] : 0.0, rsj = h ? __ldg(a.rs + j) : 0.0, rbj = h ? a.rb[j] : 0.0;
-        const double vi = fma(-mp, rsi, wi);
-        a.v[i] = vi;
-        acc = fma(rbi, vi, acc);
-        if (h) {
-          const double vj = fma(-mp, rsj, wj);
-          a.v[j] = vj;
-          acc = fma(rbj, vj, acc);
-        }
-      }
+      rows_ahead(
+          tid, stride, n, [&](int i) { return make_double3((double)m.w[i], __ldg(a.rs + i), a.rb[i]); },
+          [&](int i, const double3& o) {
+            const double vi = fma(-mp, o.y, o.x);
+            a.v[i] = vi;
+            acc = fma(o.z, vi, acc);
+          });
     } else {
       for (int i = tid; i < n; i += stride) {
         double vi = fma(-mp, __ldg(a.rs + i), spmv_diff32(a, a.pi, i));
@@ -1126,22 +1116,14 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
     alpha = red[0];
     double a2 = 0.0;
     acc = 0.0;
-    for (int i = tid; i < n; i += 2 * stride) {
-      const int j = i + stride;
-      const bool h = j < n;
-      const double vi = a.v[i], ri = a.r[i];
-      const double vj = h ? a.v[j] : 0.0, rj = h ? a.r[j] : 0.0;
-      const double si = fma(-alpha, vi, ri);
-      a.s[i] = si;
-      acc = fma(si, si, acc);
-      a2 += si;
-      if (h) {
-        const double sj = fma(-alpha, vj, rj);
-        a.s[j] = sj;
-        acc = fma(sj, sj, acc);
-        a2 += sj;
-      }
-    }
+    rows_ahead(
+        tid, stride, n, [&](int i) { return make_double2(a.v[i], a.r[i]); },
+        [&](int i, const double2& o) {
+          const double si = fma(-alpha, o.x, o.y);
+          a.s[i] = si;
+          acc = fma(si, si, acc);
+          a2 += si;
+        });
     write_partials(acc, a2, 2, part + 4 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
     reduce_partials(part + 4 * (size_t)nb, nb, 2, red, shv, [=](double* v) { v[1] = v[1] / dn; });
@@ -1162,22 +1144,14 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
     acc = 0.0;
     a2 = 0.0;
     if (use_mg) {
-      for (int i = tid; i < n; i += 2 * stride) {
-        const int j = i + stride;
-        const bool h = j < n;
-        const double wi = (double)m.w[i], rsi = __ldg(a.rs + i), si = a.s[i];
-        const double wj = h ? (double)m.w[j] : 0.0, rsj = h ? __ldg(a.rs + j) : 0.0, sj = h ? a.s[j] : 0.0;
-        const double ti = fma(-ms, rsi, wi);
-        a.t[i] = ti;
-        acc = fma(ti, si, acc);
-        a2 = fma(ti, ti, a2);
-        if (h) {
-          const double tj = fma(-ms, rsj, wj);
-          a.t[j] = tj;
-          acc = fma(tj, sj, acc);
-          a2 = fma(tj, tj, a2);
-        }
-      }
+      rows_ahead(
+          tid, stride, n, [&](int i) { return make_double3((double)m.w[i], __ldg(a.rs + i), a.s[i]); },
+          [&](int i, const double3& o) {
+            const double ti = fma(-ms, o.y, o.x);
+            a.t[i] = ti;
+            acc = fma(ti, o.z, acc);
+            a2 = fma(ti, ti, a2);
+          });
     } else {
       for (int i = tid; i < n; i += stride) {
         double ti = fma(-ms, __ldg(a.rs + i), spmv_diff32(a, a.si, i));
@@ -1194,36 +1168,24 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
     a2 = 0.0;
     // x += alpha (p_hat - mp) + omega (s_hat - ms), with the two mean shifts folded into one
     const double xshift = fma(alpha, mp, omega * ms);
-    // the preconditioned directions as FP64 (multigrid) or (hi, lo) pairs
-    auto dirs = [&](int i, double& pv, double& sv) {
-      if (use_mg) {
-        pv = pd[i];
-        sv = sd[i];
-      } else {
-        pv = join2(a.pi[i]);
-        sv = join2(a.si[i]);
-      }
+    struct XRow {
+      double p, s, x, t, sv, rb;
     };
-    for (int i = tid; i < n; i += 2 * stride) {
-      const int j = i + stride;
-      const bool h = j < n;
-      double pii, sii, pij = 0.0, sij = 0.0;
-      dirs(i, pii, sii);
-      const double xi = a.x[i], ti = a.t[i], s_i = a.s[i], rbi = a.rb[i];
-      if (h) dirs(j, pij, sij);
-      const double xj = h ? a.x[j] : 0.0, tj = h ? a.t[j] : 0.0, s_j = h ? a.s[j] : 0.0, rbj = h ? a.rb[j] : 0.0;
-      a.x[i] = fma(omega, sii, fma(alpha, pii, xi - xshift));
-      const double ri = fma(-omega, ti, s_i);
+    auto xr_update = [&](int i, const XRow& o) {
+      a.x[i] = fma(omega, o.s, fma(alpha, o.p, o.x - xshift));
+      const double ri = fma(-omega, o.t, o.sv);
       a.r[i] = ri;
       acc = fma(ri, ri, acc);
-      a2 = fma(rbi, ri, a2);
-      if (h) {
-        a.x[j] = fma(omega, sij, fma(alpha, pij, xj - xshift));
-        const double rj = fma(-omega, tj, s_j);
-        a.r[j] = rj;
-        acc = fma(rj, rj, acc);
-        a2 = fma(rbj, rj, a2);
-      }
+      a2 = fma(o.rb, ri, a2);
+    };
+    // the preconditioned directions: FP64 with the multigrid, else (hi, lo) pairs
+    if (use_mg) {
+      rows_ahead(
+          tid, stride, n, [&](int i) { return XRow{pd[i], sd[i], a.x[i], a.t[i], a.s[i], a.rb[i]}; }, xr_update);
+    } else {
+      rows_ahead(
+          tid, stride, n,
+          [&](int i) { return XRow{join2(a.pi[i]), join2(a.si[i]), a.x[i], a.t[i], a.s[i], a.rb[i]}; }, xr_update);
     }
     write_partials(acc, a2, 2, part + 8 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
@@ -1252,14 +1214,18 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mixed_mg(MgMxArgs m) {
 }
 
 // ---------------------------------------------------------------- host side
-int ppe_mg_blocks(int nsm) {
+// co-resident blocks of the FP64 (mixed = false) or the mixed multigrid solver
+int ppe_mg_blocks(int nsm, bool mixed) {
   int per = 1 << 20;
-  int o[4] = {0, 0, 0, 0};
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o[0], k_bicgstab_mg<true>, TPB, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o[1], k_bicgstab_mg<false>, TPB, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o[2], k_bicgstab_mixed_mg<true>, TPB, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o[3], k_bicgstab_mixed_mg<false>, TPB, 0);
-  for (int q = 0; q < 4; ++q) per = o[q] < per ? o[q] : per;
+  int o[2] = {0, 0};
+  if (mixed) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o[0], k_bicgstab_mixed_mg<true>, TPB, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o[1], k_bicgstab_mixed_mg<false>, TPB, 0);
+  } else {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o[0], k_bicgstab_mg<true>, TPB, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o[1], k_bicgstab_mg<false>, TPB, 0);
+  }
+  for (int q = 0; q < 2; ++q) per = o[q] < per ? o[q] : per;
   if (per < 1) per = 1;
   return per * nsm;
 }
@@ -1299,7 +1265,7 @@ void launch_ppe_mg_mixed(Ctx& x) {
   const Consts& c = x.c;
   const Dev& d = x.d;
   const int tail = mg_setup(x);
-  int nblk = x.mg_blocks;
+  int nblk = x.mg_blocks_mixed;
   const long long rows_per_block = (long long)TPB * (x.solver_rows_per_thread > 0 ? x.solver_rows_per_thread : 1);
   long long need = (c.npfb + rows_per_block - 1) / rows_per_block;
   if (need < nblk) nblk = (int)(need < 1 ? 1 : need);

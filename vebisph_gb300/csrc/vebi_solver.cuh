@@ -108,6 +108,23 @@ __device__ __forceinline__ void reduce_partials(const double* part, int nb, int 
   __syncthreads();
 }
 
+// A vector pass over the rows tid, tid + stride, ... with each row's operands loaded one row
+// ahead: load(i) returns row i's operands, body(i, ops) does the arithmetic and the stores.
+// The next row's loads are issued before the current row's arithmetic, so a warp waiting for
+// the FP64 pipe (2 lanes per clock per SM on this GPU) already has its next loads in flight.
+// Rows are visited in the same order as a plain loop, so sums come out bit for bit the same.
+template <class Load, class Body>
+__device__ __forceinline__ void rows_ahead(int tid, int stride, int n, Load load, Body body) {
+  if (tid >= n) return;
+  auto cur = load(tid);
+  for (int i = tid; i < n; i += stride) {
+    auto nxt = cur;
+    if (i + stride < n) nxt = load(i + stride);
+    body(i, cur);
+    cur = nxt;
+  }
+}
+
 // block partial of one or two values into part[q*nb + blockIdx.x]
 __device__ __forceinline__ void write_partials(double a, double b, int nval, double* part, double* sh) {
   for (int o = 16; o > 0; o >>= 1) {
