@@ -270,38 +270,16 @@ __global__ void __launch_bounds__(1024) k_mg_coarse_inverse(MgLevel K, double* i
   if (tx == 0 && ty == 0) *ok = good ? 1 : 0;
 }
 
-// sum over a row's cell pairs t = t_first..m-1 of (A P)_ic (g_c - g_own), in pair order,
-// four pairs at a time with all their loads issued before the gathers of g they index
-__device__ __forceinline__ double ap_pairs(const int* __restrict__ ragg, const double* __restrict__ rval, int m,
-                                           size_t i, size_t n, const double* g, double gc, double ap,
-                                           int t_first = 1) {
-  for (int t0 = t_first; t0 < m; t0 += 4) {
-    int c4[4];
-    double v4[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const bool ok = t0 + u < m;
-      const size_t e = (size_t)(t0 + u) * n + i;
-      c4[u] = ok ? __ldg(ragg + e) : -1;
-      v4[u] = ok ? __ldg(rval + e) : 0.0;
-    }
-    double g4[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) g4[u] = c4[u] >= 0 ? g[c4[u]] : gc;
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (c4[u] >= 0) ap = fma(v4[u], g4[u] - gc, ap);
-  }
-  return ap;
-}
-
-// rowsum_i g_own + sum_c (A P)_ic (g_c - g_own) for row i from its direction table: the eight
-// neighbour cells' values and gathers are all issued at once, their addresses computed from the
-// row's own cell (`own`, with g[own] = gc); unused directions gather g[own] and add nothing.  The
-// sum runs in the pair order of k_mg_rows (the 3x3 in key order, then the row's searched list).
+// The row's A P g in direct form, vown g_own + sum_c (A P)_ic g_c, from its direction table:
+// the eight neighbour cells' values and gathers are all issued at once, their addresses computed
+// from the row's own cell (`own`, with g[own] = gc, vown = (A P) at the own cell); unused
+// directions gather g[own] and add nothing.  The sum runs in the pair order of k_mg_rows (the
+// 3x3 in key order, then the row's searched list).  Direct form, as the FP64 row product sums
+// A_ik x_k: nine FMAs on the FP64 pipe (2 lanes per clock per SM here) where the difference
+// form took seventeen operations.
 __device__ __forceinline__ double ap_stencil(const double* __restrict__ rv9, const int* __restrict__ ragg,
                                              const double* __restrict__ rval, int rx, size_t i, size_t n,
-                                             const double* g, int own, int ncx, double gc, double rs) {
+                                             const double* g, int own, int ncx, double gc, double vown) {
   const unsigned used = ((unsigned)rx >> 16) & 0xffu;
   double v8[8], g8[8];
 #pragma unroll
@@ -311,12 +289,15 @@ __device__ __forceinline__ double ap_stencil(const double* __restrict__ rv9, con
     v8[k] = __ldg(rv9 + (size_t)k * n + i);
     g8[k] = g[(used >> k) & 1u ? own + off : own];
   }
-  double ap = rs * gc;
+  double ap = vown * gc;
 #pragma unroll
   for (int k = 0; k < 8; ++k)
-    if ((used >> k) & 1u) ap = fma(v8[k], g8[k] - gc, ap);
+    if ((used >> k) & 1u) ap = fma(v8[k], g8[k], ap);
   const int t0 = rx & 0xff, m = (rx >> 8) & 0xff;
-  if (t0 < m) ap = ap_pairs(ragg, rval, m, i, n, g, gc, ap, t0);
+  for (int t = t0; t < m; ++t) {
+    const size_t e = (size_t)t * n + i;
+    ap = fma(__ldg(rval + e), g[__ldg(ragg + e)], ap);
+  }
   return ap;
 }
 
@@ -537,14 +518,14 @@ __device__ bool mg_vcycle(const MgArgs& a, double* q, double qshift, double* out
   }
   // prolongation to the particles (the particle level is pre-smoothed only), and
   // w = A out = A z + gamma (A P) g1 with A z = q - fr from the fine residual and (A P) g1 in
-  // difference form over the row's cell pairs: rowsum_i g_own + sum_c (AP)_ic (g_c - g_own)
+  // direct form over the row's cells (ap_stencil).
   // Software-pipelined: a row's streamed operands are loaded one pass ahead, together with the
   // gathers of the row before, so each pass waits for one round trip to memory, not two.
   const double* g1 = lv_sol(a, 0);
   double acc = 0.0;
   struct Row {
     int c, rx;
-    double z, q, fr, rs;
+    double z, q, fr, vown;
   };
   auto load_row = [&](int i) {
     Row r;
@@ -553,7 +534,7 @@ __device__ bool mg_vcycle(const MgArgs& a, double* q, double qshift, double* out
     r.z = z[i];
     r.q = q[i];
     r.fr = a.fr[i];
-    r.rs = a.rsum[i];
+    r.vown = __ldg(a.rval + i);  // slot 0: the row's own cell
     return r;
   };
   Row cur{};
@@ -566,7 +547,7 @@ __device__ bool mg_vcycle(const MgArgs& a, double* q, double qshift, double* out
     if (r.c >= 0) {
       const double gc = g1[r.c];
       o = fma(MG_GAMMA, gc, o);
-      w = fma(MG_GAMMA, ap_stencil(a.rv9, a.ragg, a.rval, r.rx, i, n, g1, r.c, a.ncx, gc, r.rs), w);
+      w = fma(MG_GAMMA, ap_stencil(a.rv9, a.ragg, a.rval, r.rx, i, n, g1, r.c, a.ncx, gc, r.vown), w);
     }
     out[i] = o;
     a.w[i] = w;
@@ -770,19 +751,21 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
     omega = red[0];
     acc = 0.0;
     a2 = 0.0;
+    // x += alpha (p_hat - mp) + omega (s_hat - ms), with the two mean shifts folded into one
+    const double xshift = fma(alpha, mp, omega * ms);
     for (int i = tid; i < n; i += 2 * stride) {
       const int j = i + stride;
       const bool h = j < n;
       const double sii = a.sinv[i], pii = a.pinv[i], xi = a.x[i], ti = a.t[i], s_i = a.s[i], rbi = a.rb[i];
       const double sij = h ? a.sinv[j] : 0.0, pij = h ? a.pinv[j] : 0.0, xj = h ? a.x[j] : 0.0;
       const double tj = h ? a.t[j] : 0.0, s_j = h ? a.s[j] : 0.0, rbj = h ? a.rb[j] : 0.0;
-      a.x[i] = fma(omega, sii - ms, fma(alpha, pii - mp, xi));
+      a.x[i] = fma(omega, sii, fma(alpha, pii, xi - xshift));
       const double ri = fma(-omega, ti, s_i);
       a.r[i] = ri;
       acc = fma(ri, ri, acc);
       a2 = fma(rbi, ri, a2);
       if (h) {
-        a.x[j] = fma(omega, sij - ms, fma(alpha, pij - mp, xj));
+        a.x[j] = fma(omega, sij, fma(alpha, pij, xj - xshift));
         const double rj = fma(-omega, tj, s_j);
         a.r[j] = rj;
         acc = fma(rj, rj, acc);
