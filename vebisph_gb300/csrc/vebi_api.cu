@@ -962,6 +962,8 @@ static DView dview(Ctx& x, const std::string& nm) {
   if (nm == "theta_star") return D(d.th, n);  // theta* is the step's final theta
   if (nm == "ppe_B") return D(d.ppe_B, n);
   if (nm == "ppe_diag") return D(d.ppe_diag, n);
+  // FP64 off-diagonal values: a mixed step writes them only for rows with mirrors or smoothing
+  // (and all rows while the adjoint tapes it); its solvers read ppe_val32 and rowsum
   if (nm == "ppe_val") return D(d.ppe_val, ell);
   if (nm == "ppe_col") return I(d.ppe_col, ell);
   if (nm == "grad_px") return D(d.gpx, n);

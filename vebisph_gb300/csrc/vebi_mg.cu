@@ -820,6 +820,7 @@ struct MgMxArgs {
   float* g32;              // the level-1 solution rounded to FP32
   float* rs32;             // the row sums rounded to FP32
   float* q32;              // the V-cycle's input (after mean removal) rounded to FP32
+  const double* diag;      // the PPE matrix's FP64 diagonal
 };
 
 // sum_k A_ik (z_col - z_i) + rowsum_i z_i in FP32 (one FP32 vector; rs32 = FP32 row sums)
@@ -1020,13 +1021,10 @@ __global__ void __launch_bounds__(TPB, VEBI_MIXED_MG_BLOCKS_PER_SM) k_bicgstab_m
     return true;
   };
   for (int i = tid; i < n; i += stride) {
-    // 1/diag from the row sum and the FP32 off-diagonal values (diag = rowsum - sum_k A_ik)
-    const double rsi = __ldg(a.rs + i);
-    double dg = rsi;
-    const int cnt = __ldg(a.cnt + i);
-    for (int k = 0; k < cnt; ++k) dg -= (double)__ldg(a.val32 + (size_t)k * a.stride + i);
-    m.dinv0[i] = dg != 0.0 ? (float)(1.0 / dg) : 0.f;
-    m.rs32[i] = (float)rsi;
+    // the particle level's Jacobi sweep, in FP32: 1/diag of the assembled matrix
+    const float dg = (float)__ldg(m.diag + i);
+    m.dinv0[i] = dg != 0.f ? 1.0f / dg : 0.f;
+    m.rs32[i] = (float)__ldg(a.rs + i);
   }
   if (a.warm) {
     for (int i = tid; i < n; i += stride) {
@@ -1266,7 +1264,7 @@ void launch_ppe_mg_mixed(Ctx& x) {
                     c.warm_start},
              x.d_mg, (int)x.mg.size(), tail, d.cellpart, d.cell_start, d.cell_cnt, d.ip, (float*)x.mg_z,
              (float*)x.mg_fr, (float*)x.mg_dinv0, x.mg_ragg, x.mg_rx, x.mg_rval, (const float*)x.mg_rv9, c.ncx,
-             (float*)x.mg_w, x.mg_kinv, x.mg_kinv_ok, x.mg_g32, (float*)x.mg_rsum, x.mg_q32};
+             (float*)x.mg_w, x.mg_kinv, x.mg_kinv_ok, x.mg_g32, (float*)x.mg_rsum, x.mg_q32, d.ppe_diag};
   if (c.open_domain == 0) cudaLaunchKernelEx(&cfg, k_bicgstab_mixed_mg<true>, m);
   else cudaLaunchKernelEx(&cfg, k_bicgstab_mixed_mg<false>, m);
   x.launches++;

@@ -62,22 +62,57 @@ __global__ void k_ppe_mean(Consts c, Dev d, int nblk) {
 // columns, so one pass writes each slot once with the same value (0 + temp) the general path
 // accumulates; the first mirror neighbour sends the row to the general path, which starts over.
 // The mixed step (wL32 given) also writes the FP32 off-diagonal values and the FP64 row sums
-// diag + sum_k A_ik, in slot order, that its difference-form SpMV reads.
-__global__ void k_ppe_assemble(Consts c, Dev d, const float* __restrict__ wL32) {
+// diag + sum_k A_ik, in slot order, that its difference-form SpMV reads.  Its solvers read no
+// FP64 off-diagonal value, so a mixed row without mirrors, smoothing or a free-surface
+// condition takes a single FP32 pass: the FP32 values directly (0 + (-w) rounded to FP32 is -w,
+// +0 for a zero weight), the diagonal sum_k w_k by compensated FP32 summation (TwoSum, Knuth;
+// exact unless the sum needs more than 48 bits) widened to FP64 once, and the row sum diag +
+// sum_k A_ik, which is exactly 0 for such a row.  This GPU issues FP64 at 1/64 of the FP32 rate,
+// and the FP64 form of this pass was bound by it.  keep64 (the adjoint's recompute of a
+// recorded step, which tapes the FP64 matrix) takes the FP64 form.
+__device__ __forceinline__ double plus_zero(double x) {  // 0.0 + x without the FP64 pipe
+  const long long b = __double_as_longlong(x);
+  return __longlong_as_double(b == (long long)0x8000000000000000ull ? 0ll : b);
+}
+
+__global__ void k_ppe_assemble(Consts c, Dev d, const float* __restrict__ wL32, int keep64) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.npfb) return;
   double B = d.ppe_B[i];
   if (c.open_domain == 0) B = B - d.s->rhs_mean;
   const int cnt = d.ij_count[i];
+  const bool smooth = c.open_domain == 1 && d.n_surf[i] != 1 && d.ppe_smooth[i] != 1.0;
+  bool w64 = wL32 == nullptr || keep64 || smooth || d.n_surf[i] != 0;
   bool any_mirror = false;
   double Adiag = 0.0;
-  for (int k = 0; k < cnt; ++k) {
-    const int j = d.ij_link[ELL(k, i)];
-    if (j >= c.npfb) { any_mirror = true; break; }
-    const double temp = wL32 ? -(double)wL32[ELL(k, i)] : -d.wL[ELL(k, i)];
-    Adiag = Adiag - temp;
-    d.ppe_col[ELL(k, i)] = j;
-    d.ppe_val[ELL(k, i)] = 0.0 + temp;
+  if (!w64) {  // mixed, FP32 pass
+    float hs = 0.f, hc = 0.f;
+    for (int k = 0; k < cnt; ++k) {
+      const int j = d.ij_link[ELL(k, i)];
+      if (j >= c.npfb) { any_mirror = true; break; }
+      const float w = wL32[ELL(k, i)];
+      const float t = hs + w, bp = t - hs;
+      hc += (hs - (t - bp)) + (w - bp);
+      hs = t;
+      d.ppe_col[ELL(k, i)] = j;
+      d.ppe_val32[ELL(k, i)] = w == 0.f ? 0.f : -w;
+    }
+    if (!any_mirror) {
+      d.ppe_diag[i] = (double)hs + (double)hc;
+      d.ppe_B[i] = B;
+      d.rowsum[i] = 0.0;
+      if (c.open_domain == 1) d.bM[i] = 1.0 / (d.ppe_diag[i] + 1.0e-15);
+      return;
+    }
+  } else {
+    for (int k = 0; k < cnt; ++k) {
+      const int j = d.ij_link[ELL(k, i)];
+      if (j >= c.npfb) { any_mirror = true; break; }
+      const double temp = wL32 ? -(double)wL32[ELL(k, i)] : -d.wL[ELL(k, i)];
+      Adiag = Adiag - temp;
+      d.ppe_col[ELL(k, i)] = j;
+      d.ppe_val[ELL(k, i)] = plus_zero(temp);
+    }
   }
   if (any_mirror) {
     for (int k = 0; k < cnt; ++k) {
@@ -109,22 +144,23 @@ __global__ void k_ppe_assemble(Consts c, Dev d, const float* __restrict__ wL32) 
     }
   }
   if (d.n_surf[i] != 0) Adiag = 1.0e30;
-  d.ppe_diag[i] = 0.0 + Adiag;
-  if (c.open_domain == 1 && d.n_surf[i] != 1 && d.ppe_smooth[i] != 1.0) {
+  const double diag = 0.0 + Adiag;
+  d.ppe_diag[i] = diag;
+  if (smooth) {
     const double ps = d.ppe_smooth[i];
     B = B * ps;
     for (int k = 0; k < cnt; ++k) d.ppe_val[ELL(k, i)] = d.ppe_val[ELL(k, i)] * ps;
   }
   d.ppe_B[i] = B;
   if (wL32) {
-    double rs = d.ppe_diag[i];
+    double rs = diag;
     for (int k = 0; k < cnt; ++k) {
       const double v = d.ppe_val[ELL(k, i)];
       rs += v;
       d.ppe_val32[ELL(k, i)] = (float)v;
     }
     d.rowsum[i] = rs;
-    if (c.open_domain == 1) d.bM[i] = 1.0 / (d.ppe_diag[i] + 1.0e-15);
+    if (c.open_domain == 1) d.bM[i] = 1.0 / (diag + 1.0e-15);
   }
 }
 
@@ -348,7 +384,8 @@ void launch_ppe(Ctx& x) {
   if (mixed) launch_ppe_rhs32(x);
   else VEBI_LAUNCH(x, k_ppe_rhs, g, TPB, c, x.d);
   VEBI_LAUNCH(x, k_ppe_mean, 1, TPB, c, x.d, g);
-  VEBI_LAUNCH(x, k_ppe_assemble, g, TPB, c, x.d, mixed ? (const float*)x.d.wL32 : (const float*)nullptr);
+  VEBI_LAUNCH(x, k_ppe_assemble, g, TPB, c, x.d, mixed ? (const float*)x.d.wL32 : (const float*)nullptr,
+              x.rep_p != nullptr ? 1 : 0);
   stage_mark(x, 10);
   if (x.rep_p) {  // a recorded step recomputed by the adjoint: its solution is known
     cudaMemcpyAsync(x.d.p, x.rep_p, sizeof(double) * (size_t)c.npfb, cudaMemcpyDeviceToDevice, x.st);
