@@ -210,6 +210,12 @@ int vebi_debug_get(vebi_ctx* ctx, const char* name, void* out, int64_t bytes);
  * CUDA context stays usable. */
 int vebi_test_barrier_timeout(int32_t blocks, int64_t spin_limit, int32_t* status_out, double* ms_out);
 
+/* Self-check of the library's FP32 <-> FP64 conversions on the integer pipe against the GPU's
+ * own conversions, on n seeded inputs (1..2^32) covering every class of value: the counts of
+ * mismatching results go to *bad_narrow (FP64 -> FP32) and *bad_widen (FP32 -> FP64).  No
+ * reference counterpart. */
+int vebi_test_conversions(int64_t n, uint64_t seed, int64_t* bad_narrow, int64_t* bad_widen);
+
 /* ---- A PPE solve that allocates nothing.  No counterpart in the reference. ------------
  * For callers that cannot call cudaMalloc -- a host framework whose allocator owns all device
  * memory, or a real-time loop that must not allocate -- this runs the step's BiCGSTAB

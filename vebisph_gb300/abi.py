@@ -115,6 +115,7 @@ EXPORTED_SYMBOLS = [
     "vebi_dump_async", "vebi_dump_write", "vebi_dump_wait", "vebi_format_list",
     "vebi_set_weissenberg", "vebi_adjoint_create", "vebi_adjoint_record", "vebi_adjoint_replay",
     "vebi_adjoint_restore", "vebi_adjoint_reverse", "vebi_adjoint_destroy", "vebi_test_barrier_timeout",
+    "vebi_test_conversions",
     "vebi_set_velocity_limit", "vebi_set_coarse_block_rows",
 ]
 DUMP_BACKGROUND = 1
@@ -184,6 +185,8 @@ def load_library():
     lib.vebi_adjoint_destroy.argtypes = [vp]
     lib.vebi_test_barrier_timeout.argtypes = [C.c_int32, C.c_int64, P(C.c_int32), P(C.c_double)]
     lib.vebi_test_barrier_timeout.restype = C.c_int
+    lib.vebi_test_conversions.argtypes = [C.c_int64, C.c_uint64, P(C.c_int64), P(C.c_int64)]
+    lib.vebi_test_conversions.restype = C.c_int
     for fn in ("vebi_set_weissenberg", "vebi_adjoint_create", "vebi_adjoint_record", "vebi_adjoint_replay",
                "vebi_adjoint_restore", "vebi_adjoint_reverse", "vebi_adjoint_destroy"):
         getattr(lib, fn).restype = C.c_int

@@ -246,6 +246,38 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
 }
 
 // ---------------------------------------------------------------------------------------------
+// FP32 <-> FP64 conversions on the integer pipe.  This GPU runs conversions on its FP64 pipe
+// (2 lanes per clock per SM): measured, an FP32-to-FP64 conversion costs as much as an FP64
+// add and an FP64-to-FP32 conversion about twice that.  Both are rebuilt here from the IEEE 754
+// binary32/binary64 encodings for the normal range, bit for bit the results of the hardware
+// conversions (round to nearest even), which handle the rest (zeros, subnormals, infinities,
+// NaNs, results outside the binary32 normal range).  vebi_test_conversions checks them against
+// the hardware on every class of input.
+__device__ __forceinline__ double widen(float f) {  // == (double)f
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e - 1u < 254u) {  // normal binary32: rebias the exponent (+896), shift the mantissa by 29
+    const unsigned long long b = ((unsigned long long)(u >> 31) << 63) | ((unsigned long long)(e + 896u) << 52) |
+                                 ((unsigned long long)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)b);
+  }
+  return (double)f;
+}
+
+__device__ __forceinline__ float narrow(double d) {  // == (float)d
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+  if (e - 897u < 254u) {  // a binary32 normal exponent (a round-up may carry into infinity)
+    const unsigned long long m = b & 0x000fffffffffffffull;
+    unsigned r = ((e - 896u) << 23) | (unsigned)(m >> 29);
+    const unsigned low = (unsigned)(m & 0x1fffffffull), half = 0x10000000u;
+    r += (low > half || (low == half && (r & 1u))) ? 1u : 0u;  // the carry propagates into the exponent
+    return __uint_as_float((unsigned)(b >> 63) << 31 | r);
+  }
+  return (float)d;
+}
+
+// ---------------------------------------------------------------------------------------------
 // host side: per-context bookkeeping shared between translation units
 struct Ctx;
 void launch_advect_bin(Ctx& x);

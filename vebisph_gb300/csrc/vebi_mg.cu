@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(TPB) k_mg_rows(Consts c, Dev d, const float* _
   const int cnt = d.ij_count[i];
   for (int k = 0; k < cnt; ++k) {
     const int a = d.cellpart[d.ppe_col[ELL(k, i)]];
-    const double v = val32 ? (double)val32[ELL(k, i)] : d.ppe_val[ELL(k, i)];
+    const double v = val32 ? widen(val32[ELL(k, i)]) : d.ppe_val[ELL(k, i)];
     if (a < 0) continue;
     const int del = a - own;
     const int r = del + ncx + 1;  // row dy=-1 at 0..2, dy=0 at ncx..ncx+2, dy=+1 at 2ncx..2ncx+2
@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(TPB) k_mg_rows(Consts c, Dev d, const float* _
     if (q == 4) continue;
     const int k = q < 4 ? q : q - 1;
     const bool u = (used & (1u << q)) != 0;
-    if (val32) ((float*)rv9)[(size_t)k * c.npfb + i] = u ? (float)acc[q * TPB] : 0.f;
+    if (val32) ((float*)rv9)[(size_t)k * c.npfb + i] = u ? narrow(acc[q * TPB]) : 0.f;
     else rv9[(size_t)k * c.npfb + i] = u ? acc[q * TPB] : 0.0;
     if (!u) continue;
     used8 |= 1u << k;
@@ -358,7 +358,7 @@ __device__ __forceinline__ void lv_smooth(const MgLevel& L, int i0, int st, floa
   for (int c = i0; c < L.n; c += st) {
     const double v = fma(MG_OMEGA * __ldg(L.dinv + c), L.b[c] - lv_Ax(L, L.x, c), L.x[c]);
     L.r[c] = v;
-    if (x32) x32[c] = (float)v;
+    if (x32) x32[c] = narrow(v);
   }
 }
 
@@ -419,7 +419,7 @@ __device__ __forceinline__ void lv_prolong_smooth(const MgLevel& F, const double
     for (int t = 0; t < m; ++t) y = fma(__ldg(F.val + (size_t)t * F.n + c), xp(__ldg(F.col + (size_t)t * F.n + c)), y);
     const double v = fma(MG_OMEGA * __ldg(F.dinv + c), F.b[c] - y, xc);
     F.r[c] = v;
-    if (x32) x32[c] = (float)v;
+    if (x32) x32[c] = narrow(v);
   }
 }
 
@@ -455,7 +455,7 @@ __device__ void mg_block_levels(const MgArgs& a) {
     }
   }
   if (a.g32 && a.nl == 1) {  // level 1 is the coarsest
-    for (int c = i0; c < K.n; c += st) a.g32[c] = (float)K.x[c];
+    for (int c = i0; c < K.n; c += st) a.g32[c] = narrow(K.x[c]);
     __syncthreads();
   }
   for (int l = a.nl - 2; l >= a.tail; --l) {
@@ -896,7 +896,7 @@ __device__ bool mg_vcycle_mixed(const MgMxArgs& a, double* q, double qshift, dou
       tid, stride, n, [&](int i) { return QRow{q[i], a.dinv0[i]}; },
       [&](int i, const QRow& o) {
         const double qi = o.q - qshift;
-        const float fi = (float)qi;
+        const float fi = narrow(qi);
         q[i] = qi;
         q32[i] = fi;
         z[i] = (float)MG_OMEGA * o.d * fi;
@@ -914,7 +914,7 @@ __device__ bool mg_vcycle_mixed(const MgMxArgs& a, double* q, double qshift, dou
         if (i >= n) break;
         b32 += a.fr[i];
       }
-      const double b = (double)b32;
+      const double b = widen(b32);
       L1.b[cc] = b;
       L1.x[cc] = MG_OMEGA * __ldg(L1.dinv + cc) * b;
     }
@@ -971,7 +971,7 @@ __device__ bool mg_vcycle_mixed(const MgMxArgs& a, double* q, double qshift, dou
       oi = fmaf(gam, gc, oi);
       wi = fmaf(gam, ap_stencil32(a.rv9, a.ragg, a.rval, r.rx, i, n, g32, r.c, a.ncx, gc, r.rs), wi);
     }
-    const double od = (double)oi;
+    const double od = widen(oi);
     out[i] = od;
     a.w[i] = wi;
     acc += od;
@@ -1022,9 +1022,9 @@ __global__ void __launch_bounds__(TPB, VEBI_MIXED_MG_BLOCKS_PER_SM) k_bicgstab_m
   };
   for (int i = tid; i < n; i += stride) {
     // the particle level's Jacobi sweep, in FP32: 1/diag of the assembled matrix
-    const float dg = (float)__ldg(m.diag + i);
+    const float dg = narrow(__ldg(m.diag + i));
     m.dinv0[i] = dg != 0.f ? 1.0f / dg : 0.f;
-    m.rs32[i] = (float)__ldg(a.rs + i);
+    m.rs32[i] = narrow(__ldg(a.rs + i));
   }
   if (a.warm) {
     for (int i = tid; i < n; i += stride) {
@@ -1078,7 +1078,7 @@ __global__ void __launch_bounds__(TPB, VEBI_MIXED_MG_BLOCKS_PER_SM) k_bicgstab_m
     acc = 0.0;
     if (use_mg) {
       rows_ahead(
-          tid, stride, n, [&](int i) { return make_double3((double)m.w[i], __ldg(a.rs + i), a.rb[i]); },
+          tid, stride, n, [&](int i) { return make_double3(widen(m.w[i]), __ldg(a.rs + i), a.rb[i]); },
           [&](int i, const double3& o) {
             const double vi = fma(-mp, o.y, o.x);
             a.v[i] = vi;
@@ -1126,7 +1126,7 @@ __global__ void __launch_bounds__(TPB, VEBI_MIXED_MG_BLOCKS_PER_SM) k_bicgstab_m
     a2 = 0.0;
     if (use_mg) {
       rows_ahead(
-          tid, stride, n, [&](int i) { return make_double3((double)m.w[i], __ldg(a.rs + i), a.s[i]); },
+          tid, stride, n, [&](int i) { return make_double3(widen(m.w[i]), __ldg(a.rs + i), a.s[i]); },
           [&](int i, const double3& o) {
             const double ti = fma(-ms, o.y, o.x);
             a.t[i] = ti;

@@ -699,3 +699,73 @@ extern "C" int vebi_test_barrier_timeout(int32_t blocks, int64_t spin_limit, int
   if (ms_out) *ms_out = ms;
   return VEBI_OK;
 }
+
+// Check of the integer-pipe conversions (vebi_common.cuh: widen, narrow) against the hardware
+// conversions: every thread draws one 64-bit and one 32-bit pattern from a SplitMix64 stream
+// and, in turn, covers random patterns of every class, doubles whose exponent lies around the
+// binary32 range (including exact halfway cases and the largest binary32 values), and exact
+// zeros; results are compared bit for bit (NaN against NaN).
+namespace vebi {
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+__global__ void k_conversion_check(long long n, unsigned long long seed, unsigned int* bad) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    unsigned long long b = splitmix64(seed ^ (unsigned long long)t * 0x632be59bd9b4e019ull);
+    const unsigned long long r2 = splitmix64(b);
+    switch (t & 7) {
+      case 0: case 1: break;  // any 64-bit pattern
+      case 2: case 3: {       // exponent 880..1167 around the binary32 range
+        const unsigned long long e = 880 + (r2 % 288);
+        b = (b & 0x800fffffffffffffull) | (e << 52);
+        break;
+      }
+      case 4: {  // exact halfway between two binary32 values (low 29 bits 0x10000000)
+        const unsigned long long e = 890 + (r2 % 270);
+        b = (b & 0x800fffffe0000000ull) | (e << 52) | 0x10000000ull;
+        break;
+      }
+      case 5: {  // at and next to the largest binary32 magnitudes, and the smallest normals
+        const unsigned long long e = (r2 & 1) ? 1150 : 897;
+        b = (b & 0x8000000000000000ull) | (e << 52) | (0x000fffffe0000000ull + (r2 >> 1) % 0x40000000ull);
+        break;
+      }
+      case 6: b &= 0x8000000000000000ull; break;  // signed zeros
+      default: b = (b & 0x800fffffffffffffull) | ((unsigned long long)(r2 % 2048) << 52); break;
+    }
+    const double d = __longlong_as_double((long long)b);
+    const float fh = (float)d, fs = narrow(d);
+    const bool okn = (fh != fh) ? (fs != fs) : __float_as_uint(fh) == __float_as_uint(fs);
+    const float f = __uint_as_float((unsigned)r2 ^ (unsigned)(b >> 32));
+    const double dh = (double)f, ds = widen(f);
+    const bool okw = (dh != dh) ? (ds != ds) : __double_as_longlong(dh) == __double_as_longlong(ds);
+    if (!okn) atomicAdd(bad, 1u);
+    if (!okw) atomicAdd(bad + 1, 1u);
+  }
+}
+}  // namespace vebi
+
+extern "C" int vebi_test_conversions(int64_t n, uint64_t seed, int64_t* bad_narrow, int64_t* bad_widen) {
+  using namespace vebi;
+  if (n < 1 || n > (1ll << 32) || !bad_narrow || !bad_widen) {
+    vebi_set_last_error_internal("vebi_test_conversions: n in 1..2^32, bad_narrow, bad_widen");
+    return VEBI_ERR_ARG;
+  }
+  unsigned int* bad = nullptr;
+  cudaError_t e = cudaMalloc(&bad, 2 * sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMemset(bad, 0, 2 * sizeof(unsigned int));
+  if (e == cudaSuccess) {
+    k_conversion_check<<<1024, 256>>>((long long)n, (unsigned long long)seed, bad);
+    e = cudaGetLastError();
+  }
+  unsigned int h[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(h, bad, sizeof(h), cudaMemcpyDeviceToHost);
+  if (bad) cudaFree(bad);
+  if (e != cudaSuccess) { vebi_set_last_error_internal(cudaGetErrorString(e)); return VEBI_ERR_CUDA; }
+  *bad_narrow = h[0];
+  *bad_widen = h[1];
+  return VEBI_OK;
+}

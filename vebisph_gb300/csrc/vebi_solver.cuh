@@ -203,11 +203,12 @@ struct MxArgs {
   int warm;
 };
 
+// (hi, lo) FP32 pair of a double and back; conversions on the integer pipe (widen, narrow)
 __device__ __forceinline__ float2 split2(double v) {
-  float h = (float)v;
-  return make_float2(h, (float)(v - (double)h));
+  const float h = narrow(v);
+  return make_float2(h, narrow(v - widen(h)));
 }
-__device__ __forceinline__ double join2(float2 q) { return (double)q.x + (double)q.y; }
+__device__ __forceinline__ double join2(float2 q) { return widen(q.x) + widen(q.y); }
 
 __device__ __forceinline__ double spmv_diff32(const MxArgs& a, const float2* xv, int i) {
   const int cnt = __ldg(a.cnt + i);
@@ -234,7 +235,7 @@ __device__ __forceinline__ double spmv_diff32(const MxArgs& a, const float2* xv,
     cp += st;
     vp += st;
   }
-  return fma(__ldg(a.rs + i), join2(xi), (double)((b0 + b1) + (b2 + b3)));
+  return fma(__ldg(a.rs + i), join2(xi), widen((b0 + b1) + (b2 + b3)));
 }
 
 }  // namespace vebi

@@ -151,8 +151,8 @@ __global__ void k_split_fields(Dev d, SplitArgs a) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x)
     for (int f = 0; f < a.nf; ++f) {
       const double v = a.src[f][i];
-      const float h = (float)v;
-      a.dst[f][i] = make_float2(h, (float)(v - (double)h));
+      const float h = narrow(v);  // (float)v, (float)(v - (double)h) on the integer pipe
+      a.dst[f][i] = make_float2(h, narrow(v - widen(h)));
     }
 }
 
