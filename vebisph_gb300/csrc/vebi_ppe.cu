@@ -238,13 +238,17 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
       if (!grid_sync(s)) return;
       reduce_partials(slot, nb, 1, red, shv, [=](double* v) { v[0] = v[0] / dn; });
       const double mean = red[0];
-      for (int i = tid; i < n; i += stride) {
-        double pi = a.p[i] - mean;
-        a.p[i] = pi;
-        a.pinv[i] = pi * rinv1;
-      }
+      rows_ahead(
+          tid, stride, n, [&](int i) { return a.p[i]; },
+          [&](int i, double p) {
+            const double pi = p - mean;
+            a.p[i] = pi;
+            a.pinv[i] = pi * rinv1;
+          });
     } else {
-      for (int i = tid; i < n; i += stride) a.pinv[i] = a.p[i] * a.rinvM[i];
+      rows_ahead(
+          tid, stride, n, [&](int i) { return make_double2(a.p[i], a.rinvM[i]); },
+          [&](int i, const double2& o) { a.pinv[i] = o.x * o.y; });
     }
     if (!grid_sync(s)) return;
     // v = A p_inv ; (r_bar, v)
@@ -292,11 +296,13 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
       break;
     }
     // s -= mean (closed) ; s_inv
-    for (int i = tid; i < n; i += stride) {
-      double si = a.s[i];
-      if (NONULL) { si = si - mean_s; a.s[i] = si; }
-      a.sinv[i] = NONULL ? si * rinv1 : si * a.rinvM[i];
-    }
+    rows_ahead(
+        tid, stride, n, [&](int i) { return make_double2(a.s[i], NONULL ? rinv1 : a.rinvM[i]); },
+        [&](int i, const double2& o) {
+          double si = o.x;
+          if (NONULL) { si = si - mean_s; a.s[i] = si; }
+          a.sinv[i] = si * o.y;
+        });
     if (!grid_sync(s)) return;
     // t = A s_inv ; (t, s) ; |t|^2
     acc = 0.0;
@@ -507,11 +513,14 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab_mixed(MxArgs a) {
   while (iter <= a.itermax) {
     if (rho == 0.0) { warn |= VEBI_WARN_BICGSTAB_BREAKDOWN; done = true; break; }
     acc = 0.0;
-    for (int i = tid; i < n; i += stride) {
-      double pi = (iter == 1) ? a.r[i] : fma(beta, fma(-omega, a.v[i], a.p[i]), a.r[i]);
-      a.p[i] = pi;
-      acc += pi;
-    }
+    // vector passes: each row's operands loaded one row ahead (rows_ahead)
+    rows_ahead(
+        tid, stride, n, [&](int i) { return make_double3(a.r[i], a.v[i], a.p[i]); },
+        [&](int i, const double3& o) {
+          const double pi = (iter == 1) ? o.x : fma(beta, fma(-omega, o.y, o.z), o.x);
+          a.p[i] = pi;
+          acc += pi;
+        });
     double mean = 0.0;
     if (NONULL) {
       write_partials(acc, 0.0, 1, part, sh);
@@ -519,11 +528,13 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab_mixed(MxArgs a) {
       reduce_partials(part, nb, 1, red, shv, [=](double* v) { v[0] = v[0] / dn; });
       mean = red[0];
     }
-    for (int i = tid; i < n; i += stride) {
-      double pi = a.p[i];
-      if (NONULL) { pi = pi - mean; a.p[i] = pi; }
-      a.pi[i] = split2(NONULL ? pi * rinv1 : pi * a.rinvM[i]);
-    }
+    rows_ahead(
+        tid, stride, n, [&](int i) { return make_double2(a.p[i], NONULL ? rinv1 : a.rinvM[i]); },
+        [&](int i, const double2& o) {
+          double pi = o.x;
+          if (NONULL) { pi = pi - mean; a.p[i] = pi; }
+          a.pi[i] = split2(pi * o.y);
+        });
     if (!grid_sync(s)) return;
     acc = 0.0;
     for (int i = tid; i < n; i += stride) {
@@ -537,12 +548,14 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab_mixed(MxArgs a) {
     alpha = red[0];
     double a2 = 0.0;
     acc = 0.0;
-    for (int i = tid; i < n; i += stride) {
-      double si = fma(-alpha, a.v[i], a.r[i]);
-      a.s[i] = si;
-      acc = fma(si, si, acc);
-      a2 += si;
-    }
+    rows_ahead(
+        tid, stride, n, [&](int i) { return make_double2(a.v[i], a.r[i]); },
+        [&](int i, const double2& o) {
+          const double si = fma(-alpha, o.x, o.y);
+          a.s[i] = si;
+          acc = fma(si, si, acc);
+          a2 += si;
+        });
     write_partials(acc, a2, 2, part + 4 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
     reduce_partials(part + 4 * (size_t)nb, nb, 2, red, shv, [=](double* v) { v[1] = v[1] / dn; });
@@ -555,11 +568,13 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab_mixed(MxArgs a) {
       done = true;
       break;
     }
-    for (int i = tid; i < n; i += stride) {
-      double si = a.s[i];
-      if (NONULL) { si = si - mean_s; a.s[i] = si; }
-      a.si[i] = split2(NONULL ? si * rinv1 : si * a.rinvM[i]);
-    }
+    rows_ahead(
+        tid, stride, n, [&](int i) { return make_double2(a.s[i], NONULL ? rinv1 : a.rinvM[i]); },
+        [&](int i, const double2& o) {
+          double si = o.x;
+          if (NONULL) { si = si - mean_s; a.s[i] = si; }
+          a.si[i] = split2(si * o.y);
+        });
     if (!grid_sync(s)) return;
     acc = 0.0;
     a2 = 0.0;
@@ -575,13 +590,19 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab_mixed(MxArgs a) {
     omega = red[0];
     acc = 0.0;
     a2 = 0.0;
-    for (int i = tid; i < n; i += stride) {
-      a.x[i] = fma(omega, join2(a.si[i]), fma(alpha, join2(a.pi[i]), a.x[i]));
-      double ri = fma(-omega, a.t[i], a.s[i]);
-      a.r[i] = ri;
-      acc = fma(ri, ri, acc);
-      a2 = fma(a.rb[i], ri, a2);
-    }
+    struct XRow {
+      float2 s, p;
+      double x, t, sv, rb;
+    };
+    rows_ahead(
+        tid, stride, n, [&](int i) { return XRow{a.si[i], a.pi[i], a.x[i], a.t[i], a.s[i], a.rb[i]}; },
+        [&](int i, const XRow& o) {
+          a.x[i] = fma(omega, join2(o.s), fma(alpha, join2(o.p), o.x));
+          const double ri = fma(-omega, o.t, o.sv);
+          a.r[i] = ri;
+          acc = fma(ri, ri, acc);
+          a2 = fma(o.rb, ri, a2);
+        });
     write_partials(acc, a2, 2, part + 8 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
     // v[2] = the relative residual, v[3] = the next iteration's beta from the new rho v[1]
