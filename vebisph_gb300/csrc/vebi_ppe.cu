@@ -214,24 +214,17 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
   const double dn = (double)n;
   while (iter <= a.itermax) {
     if (rho == 0.0) { warn |= VEBI_WARN_BICGSTAB_BREAKDOWN; done = true; break; }
-    // p = r + beta (p - omega v).  The vector passes take rows i and i + stride per thread (the
-    // rows a thread owns do not change) and issue their loads before their stores: the compiler
-    // cannot move a load of one array above a store to another that may alias it.
+    // p = r + beta (p - omega v).  The vector passes load each row's operands one row ahead
+    // (rows_ahead), so a row's loads are in flight before the previous row's stores: the
+    // compiler cannot move a load of one array above a store to another that may alias it.
     acc = 0.0;
-    for (int i = tid; i < n; i += 2 * stride) {
-      const int j = i + stride;
-      const bool h = j < n;
-      const double ri = a.r[i], vi = a.v[i], pi0 = a.p[i];
-      const double rj = h ? a.r[j] : 0.0, vj = h ? a.v[j] : 0.0, pj0 = h ? a.p[j] : 0.0;
-      const double pi = (iter == 1) ? ri : fma(beta, fma(-omega, vi, pi0), ri);
-      a.p[i] = pi;
-      acc += pi;
-      if (h) {
-        const double pj = (iter == 1) ? rj : fma(beta, fma(-omega, vj, pj0), rj);
-        a.p[j] = pj;
-        acc += pj;
-      }
-    }
+    rows_ahead(
+        tid, stride, n, [&](int i) { return make_double3(a.r[i], a.v[i], a.p[i]); },
+        [&](int i, const double3& o) {
+          const double pi = (iter == 1) ? o.x : fma(beta, fma(-omega, o.y, o.z), o.x);
+          a.p[i] = pi;
+          acc += pi;
+        });
     double* slot = part;
     if (NONULL) {
       write_partials(acc, 0.0, 1, slot, sh);
@@ -266,22 +259,14 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
     // s = r - alpha v ; |s|^2 ; sum(s)
     double a2 = 0.0;
     acc = 0.0;
-    for (int i = tid; i < n; i += 2 * stride) {
-      const int j = i + stride;
-      const bool h = j < n;
-      const double vi = a.v[i], ri = a.r[i];
-      const double vj = h ? a.v[j] : 0.0, rj = h ? a.r[j] : 0.0;
-      const double si = fma(-alpha, vi, ri);
-      a.s[i] = si;
-      acc = fma(si, si, acc);
-      a2 += si;
-      if (h) {
-        const double sj = fma(-alpha, vj, rj);
-        a.s[j] = sj;
-        acc = fma(sj, sj, acc);
-        a2 += sj;
-      }
-    }
+    rows_ahead(
+        tid, stride, n, [&](int i) { return make_double2(a.v[i], a.r[i]); },
+        [&](int i, const double2& o) {
+          const double si = fma(-alpha, o.x, o.y);
+          a.s[i] = si;
+          acc = fma(si, si, acc);
+          a2 += si;
+        });
     slot = part + 4 * (size_t)nb;
     write_partials(acc, a2, 2, slot, sh);
     if (!grid_sync(s)) return;
@@ -321,25 +306,18 @@ __global__ void __launch_bounds__(TPB, 5) k_bicgstab(BiArgs a) {
     // x, r update ; |r|^2 ; (r_bar, r) for the next rho
     acc = 0.0;
     a2 = 0.0;
-    for (int i = tid; i < n; i += 2 * stride) {
-      const int j = i + stride;
-      const bool h = j < n;
-      const double sii = a.sinv[i], pii = a.pinv[i], xi = a.x[i], ti = a.t[i], s_i = a.s[i], rbi = a.rb[i];
-      const double sij = h ? a.sinv[j] : 0.0, pij = h ? a.pinv[j] : 0.0, xj = h ? a.x[j] : 0.0;
-      const double tj = h ? a.t[j] : 0.0, s_j = h ? a.s[j] : 0.0, rbj = h ? a.rb[j] : 0.0;
-      a.x[i] = fma(omega, sii, fma(alpha, pii, xi));
-      const double ri = fma(-omega, ti, s_i);
-      a.r[i] = ri;
-      acc = fma(ri, ri, acc);
-      a2 = fma(rbi, ri, a2);
-      if (h) {
-        a.x[j] = fma(omega, sij, fma(alpha, pij, xj));
-        const double rj = fma(-omega, tj, s_j);
-        a.r[j] = rj;
-        acc = fma(rj, rj, acc);
-        a2 = fma(rbj, rj, a2);
-      }
-    }
+    struct XRow {
+      double s, p, x, t, sv, rb;
+    };
+    rows_ahead(
+        tid, stride, n, [&](int i) { return XRow{a.sinv[i], a.pinv[i], a.x[i], a.t[i], a.s[i], a.rb[i]}; },
+        [&](int i, const XRow& o) {
+          a.x[i] = fma(omega, o.s, fma(alpha, o.p, o.x));
+          const double ri = fma(-omega, o.t, o.sv);
+          a.r[i] = ri;
+          acc = fma(ri, ri, acc);
+          a2 = fma(o.rb, ri, a2);
+        });
     slot = part + 8 * (size_t)nb;
     write_partials(acc, a2, 2, slot, sh);
     if (!grid_sync(s)) return;
