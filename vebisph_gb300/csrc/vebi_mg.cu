@@ -469,25 +469,20 @@ __device__ void mg_block_levels(const MgArgs& a) {
 
 // out = M^-1 q by one V-cycle; the last loop also writes the block partial of sum(out) into
 // slot.  q needs only its own rows complete (the calling thread wrote them).
-// q -= qshift first (the closed domain's mean removal), stored back.  As in the mixed solver,
-// the vector passes take rows i and i + stride per thread and issue their loads first.
+// q -= qshift first (the closed domain's mean removal), stored back.  As in the solvers, the
+// vector passes load each row's operands one row ahead (rows_ahead).
 __device__ bool mg_vcycle(const MgArgs& a, double* q, double qshift, double* out, double* slot, double* sh,
                           int tid, int stride) {
   const int n = a.b.n;
   Scal* s = a.b.sc;
   double* z = a.z;
-  for (int i = tid; i < n; i += 2 * stride) {
-    const int j = i + stride;
-    const bool h = j < n;
-    const double qi = q[i] - qshift, qj = h ? q[j] - qshift : 0.0;
-    const double di = a.dinv0[i], dj = h ? a.dinv0[j] : 0.0;
-    q[i] = qi;
-    z[i] = MG_OMEGA * di * qi;
-    if (h) {
-      q[j] = qj;
-      z[j] = MG_OMEGA * dj * qj;
-    }
-  }
+  rows_ahead(
+      tid, stride, n, [&](int i) { return make_double2(q[i], a.dinv0[i]); },
+      [&](int i, const double2& o) {
+        const double qi = o.x - qshift;
+        q[i] = qi;
+        z[i] = MG_OMEGA * o.y * qi;
+      });
   if (!grid_sync(s)) return false;
   for (int i = tid; i < n; i += stride) a.fr[i] = q[i] - spmv_row(a.b, z, i);
   if (!grid_sync(s)) return false;
@@ -629,20 +624,14 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
   while (iter <= a.itermax) {
     if (rho == 0.0) { warn |= VEBI_WARN_BICGSTAB_BREAKDOWN; done = true; break; }
     acc = 0.0;
-    for (int i = tid; i < n; i += 2 * stride) {
-      const int j = i + stride;
-      const bool h = j < n;
-      const double ri = a.r[i], vi = a.v[i], pi = a.p[i];
-      const double rj = h ? a.r[j] : 0.0, vj = h ? a.v[j] : 0.0, pj = h ? a.p[j] : 0.0;
-      const double ni = (iter == 1) ? ri : fma(beta, fma(-omega, vi, pi), ri);
-      a.p[i] = ni;
-      acc += ni;
-      if (h) {
-        const double nj = (iter == 1) ? rj : fma(beta, fma(-omega, vj, pj), rj);
-        a.p[j] = nj;
-        acc += nj;
-      }
-    }
+    // the vector passes load each row's operands one row ahead (rows_ahead)
+    rows_ahead(
+        tid, stride, n, [&](int i) { return make_double3(a.r[i], a.v[i], a.p[i]); },
+        [&](int i, const double3& o) {
+          const double ni = (iter == 1) ? o.x : fma(beta, fma(-omega, o.y, o.z), o.x);
+          a.p[i] = ni;
+          acc += ni;
+        });
     double mean = 0.0;
     if (NONULL) {
       write_partials(acc, 0.0, 1, part, sh);
@@ -658,20 +647,13 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
     // v = A (p_hat - mp) ; (r_bar, v)
     acc = 0.0;
     if (use_mg) {
-      for (int i = tid; i < n; i += 2 * stride) {
-        const int j = i + stride;
-        const bool h = j < n;
-        const double wi = m.w[i], rsi = m.rsum[i], rbi = a.rb[i];
-        const double wj = h ? m.w[j] : 0.0, rsj = h ? m.rsum[j] : 0.0, rbj = h ? a.rb[j] : 0.0;
-        const double vi = fma(-mp, rsi, wi);
-        a.v[i] = vi;
-        acc = fma(rbi, vi, acc);
-        if (h) {
-          const double vj = fma(-mp, rsj, wj);
-          a.v[j] = vj;
-          acc = fma(rbj, vj, acc);
-        }
-      }
+      rows_ahead(
+          tid, stride, n, [&](int i) { return make_double3(m.w[i], m.rsum[i], a.rb[i]); },
+          [&](int i, const double3& o) {
+            const double vi = fma(-mp, o.y, o.x);
+            a.v[i] = vi;
+            acc = fma(o.z, vi, acc);
+          });
     } else {
       for (int i = tid; i < n; i += stride) {
         double vi = fma(-mp, m.rsum[i], spmv_row(a, a.pinv, i));
@@ -685,22 +667,14 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
     alpha = red[0];
     double a2 = 0.0;
     acc = 0.0;
-    for (int i = tid; i < n; i += 2 * stride) {
-      const int j = i + stride;
-      const bool h = j < n;
-      const double vi = a.v[i], ri = a.r[i];
-      const double vj = h ? a.v[j] : 0.0, rj = h ? a.r[j] : 0.0;
-      const double si = fma(-alpha, vi, ri);
-      a.s[i] = si;
-      acc = fma(si, si, acc);
-      a2 += si;
-      if (h) {
-        const double sj = fma(-alpha, vj, rj);
-        a.s[j] = sj;
-        acc = fma(sj, sj, acc);
-        a2 += sj;
-      }
-    }
+    rows_ahead(
+        tid, stride, n, [&](int i) { return make_double2(a.v[i], a.r[i]); },
+        [&](int i, const double2& o) {
+          const double si = fma(-alpha, o.x, o.y);
+          a.s[i] = si;
+          acc = fma(si, si, acc);
+          a2 += si;
+        });
     write_partials(acc, a2, 2, part + 4 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
     reduce_partials(part + 4 * (size_t)nb, nb, 2, red, shv, [=](double* v) { v[1] = v[1] / dn; });
@@ -721,22 +695,14 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
     acc = 0.0;
     a2 = 0.0;
     if (use_mg) {
-      for (int i = tid; i < n; i += 2 * stride) {
-        const int j = i + stride;
-        const bool h = j < n;
-        const double wi = m.w[i], rsi = m.rsum[i], si = a.s[i];
-        const double wj = h ? m.w[j] : 0.0, rsj = h ? m.rsum[j] : 0.0, sj = h ? a.s[j] : 0.0;
-        const double ti = fma(-ms, rsi, wi);
-        a.t[i] = ti;
-        acc = fma(ti, si, acc);
-        a2 = fma(ti, ti, a2);
-        if (h) {
-          const double tj = fma(-ms, rsj, wj);
-          a.t[j] = tj;
-          acc = fma(tj, sj, acc);
-          a2 = fma(tj, tj, a2);
-        }
-      }
+      rows_ahead(
+          tid, stride, n, [&](int i) { return make_double3(m.w[i], m.rsum[i], a.s[i]); },
+          [&](int i, const double3& o) {
+            const double ti = fma(-ms, o.y, o.x);
+            a.t[i] = ti;
+            acc = fma(ti, o.z, acc);
+            a2 = fma(ti, ti, a2);
+          });
     } else {
       for (int i = tid; i < n; i += stride) {
         double ti = fma(-ms, m.rsum[i], spmv_row(a, a.sinv, i));
@@ -753,25 +719,18 @@ __global__ void __launch_bounds__(TPB, 4) k_bicgstab_mg(MgArgs m) {
     a2 = 0.0;
     // x += alpha (p_hat - mp) + omega (s_hat - ms), with the two mean shifts folded into one
     const double xshift = fma(alpha, mp, omega * ms);
-    for (int i = tid; i < n; i += 2 * stride) {
-      const int j = i + stride;
-      const bool h = j < n;
-      const double sii = a.sinv[i], pii = a.pinv[i], xi = a.x[i], ti = a.t[i], s_i = a.s[i], rbi = a.rb[i];
-      const double sij = h ? a.sinv[j] : 0.0, pij = h ? a.pinv[j] : 0.0, xj = h ? a.x[j] : 0.0;
-      const double tj = h ? a.t[j] : 0.0, s_j = h ? a.s[j] : 0.0, rbj = h ? a.rb[j] : 0.0;
-      a.x[i] = fma(omega, sii, fma(alpha, pii, xi - xshift));
-      const double ri = fma(-omega, ti, s_i);
-      a.r[i] = ri;
-      acc = fma(ri, ri, acc);
-      a2 = fma(rbi, ri, a2);
-      if (h) {
-        a.x[j] = fma(omega, sij, fma(alpha, pij, xj - xshift));
-        const double rj = fma(-omega, tj, s_j);
-        a.r[j] = rj;
-        acc = fma(rj, rj, acc);
-        a2 = fma(rbj, rj, a2);
-      }
-    }
+    struct XRow {
+      double s, p, x, t, sv, rb;
+    };
+    rows_ahead(
+        tid, stride, n, [&](int i) { return XRow{a.sinv[i], a.pinv[i], a.x[i], a.t[i], a.s[i], a.rb[i]}; },
+        [&](int i, const XRow& o) {
+          a.x[i] = fma(omega, o.s, fma(alpha, o.p, o.x - xshift));
+          const double ri = fma(-omega, o.t, o.sv);
+          a.r[i] = ri;
+          acc = fma(ri, ri, acc);
+          a2 = fma(o.rb, ri, a2);
+        });
     write_partials(acc, a2, 2, part + 8 * (size_t)nb, sh);
     if (!grid_sync(s)) return;
     // v[2] = the relative residual, v[3] = the next iteration's beta from the new rho v[1]
@@ -877,10 +836,10 @@ __device__ __forceinline__ float ap_stencil32(const float* __restrict__ rv9, con
   return ap;
 }
 
-// out = M^-1 q in FP64 (the preconditioned direction); block partial of sum(out) into slot
-// The vector passes of this solver take two rows per thread per pass, i and i + stride (the
-// rows each thread owns stay the same), and issue all of a pass's loads before its stores: the
-// compiler cannot move a load above a store to another array it may alias.
+// out = M^-1 q in FP64 (the preconditioned direction); block partial of sum(out) into slot.
+// The vector passes load each row's operands one row ahead (rows_ahead), so a pass's loads are
+// in flight before the previous row's stores: the compiler cannot move a load above a store
+// to another array it may alias.
 __device__ bool mg_vcycle_mixed(const MgMxArgs& a, double* q, double qshift, double* out, double* slot,
                                 double* sh, int tid, int stride) {
   const int n = a.b.n;
