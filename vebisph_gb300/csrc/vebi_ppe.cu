@@ -85,33 +85,55 @@ __global__ void k_ppe_assemble(Consts c, Dev d, const float* __restrict__ wL32, 
   bool w64 = wL32 == nullptr || keep64 || smooth || d.n_surf[i] != 0;
   bool any_mirror = false;
   double Adiag = 0.0;
-  if (!w64) {  // mixed, FP32 pass
+  if (!w64) {  // mixed, FP32 pass, four slots at a time with their loads ahead of their stores
     float hs = 0.f, hc = 0.f;
-    for (int k = 0; k < cnt; ++k) {
-      const int j = d.ij_link[ELL(k, i)];
-      if (j >= c.npfb) { any_mirror = true; break; }
-      const float w = wL32[ELL(k, i)];
-      const float t = hs + w, bp = t - hs;
-      hc += (hs - (t - bp)) + (w - bp);
-      hs = t;
-      d.ppe_col[ELL(k, i)] = j;
-      d.ppe_val32[ELL(k, i)] = w == 0.f ? 0.f : -w;
+    for (int k0 = 0; k0 < cnt && !any_mirror; k0 += 4) {
+      int j4[4];
+      float w4[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const bool in = k0 + u < cnt;
+        j4[u] = in ? d.ij_link[ELL(k0 + u, i)] : 0;
+        w4[u] = in ? wL32[ELL(k0 + u, i)] : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (k0 + u >= cnt) break;
+        const int j = j4[u];
+        const float w = w4[u];
+        any_mirror |= j >= c.npfb;  // such a row starts over in the general path below
+        const float t = hs + w, bp = t - hs;
+        hc += (hs - (t - bp)) + (w - bp);
+        hs = t;
+        d.ppe_col[ELL(k0 + u, i)] = j;
+        d.ppe_val32[ELL(k0 + u, i)] = w == 0.f ? 0.f : -w;
+      }
     }
     if (!any_mirror) {
-      d.ppe_diag[i] = (double)hs + (double)hc;
+      d.ppe_diag[i] = widen(hs) + widen(hc);
       d.ppe_B[i] = B;
       d.rowsum[i] = 0.0;
       if (c.open_domain == 1) d.bM[i] = 1.0 / (d.ppe_diag[i] + 1.0e-15);
       return;
     }
-  } else {
-    for (int k = 0; k < cnt; ++k) {
-      const int j = d.ij_link[ELL(k, i)];
-      if (j >= c.npfb) { any_mirror = true; break; }
-      const double temp = wL32 ? -(double)wL32[ELL(k, i)] : -d.wL[ELL(k, i)];
-      Adiag = Adiag - temp;
-      d.ppe_col[ELL(k, i)] = j;
-      d.ppe_val[ELL(k, i)] = plus_zero(temp);
+  } else {  // FP64 pass, four slots at a time as above
+    for (int k0 = 0; k0 < cnt && !any_mirror; k0 += 4) {
+      int j4[4];
+      double t4[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const bool in = k0 + u < cnt;
+        j4[u] = in ? d.ij_link[ELL(k0 + u, i)] : 0;
+        t4[u] = in ? (wL32 ? -widen(wL32[ELL(k0 + u, i)]) : -d.wL[ELL(k0 + u, i)]) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (k0 + u >= cnt) break;
+        any_mirror |= j4[u] >= c.npfb;  // such a row starts over in the general path below
+        Adiag = Adiag - t4[u];
+        d.ppe_col[ELL(k0 + u, i)] = j4[u];
+        d.ppe_val[ELL(k0 + u, i)] = plus_zero(t4[u]);
+      }
     }
   }
   if (any_mirror) {
